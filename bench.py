@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""Benchmark: Landau gauge fixing of a 32^4 SU(3) lattice on one GB300.
+
+One step = one complete gauge-fixing solve: the mixed-precision checkerboard
+overrelaxation (FP32 12-real sweeps with FP64-accumulated checks, then FP64
+polish sweeps) from the same random gauge start until theta = (1/3V) sum tr[DD^+]
+< 1e-12, verified in FP64.  The links (beta = 6.0, heatbath-thermalized on the GPU
+from a cold start) and the starting transformation are generated once before the
+timed region.
+
+  value : OR site updates per second over the K timed steps, inputs resident in HBM
+  e2e   : the same metric through the public C ABI with host buffers -- H2D of
+          the links and the start transformation from pinned memory, the solve,
+          D2H of the gauge transformation -- every step
+  time_to_theta_s : mixed vs all-FP64 solve of the same problem
+
+`--impl reference` times the CPU restatement of the reference's OR update (the
+reference has no CPU overrelaxation; its observables are host C) on all host
+cores, on a bounded sample of sweeps of the same lattice.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "OR site-updates/s & time to θ<1e-12 (32^4 Landau), mixed vs FP64 on 1 GB300"
+UNIT = "site-updates/s"
+# algorithmic bytes of one OR site update, FP32 12-real storage: 8 links (96 reals)
+# + g of this parity read and written (24) + g of the other parity read once (12)
+BYTES_PER_UPDATE_FP32 = 132 * 4
+BYTES_PER_UPDATE_FP64 = 132 * 8
+FLOP_PER_UPDATE = 4766  # the reference's count (overrelax.cu:897)
+# DRAM bytes per FP32 half-sweep launch at 32^4, read+write, from the ncu capture
+# summarised in profiles/or_halfsweep_fp32_32x4.md (None until captured)
+NCU_TRAFFIC_FP32 = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gfx", choices=["gfx", "reference"])
+    ap.add_argument("--dims", default="32,32,32,32")
+    ap.add_argument("--therm", type=int, default=50, help="heatbath sweeps for the links")
+    ap.add_argument("--beta", type=float, default=6.0)
+    ap.add_argument("--eps", type=float, default=1e-12)
+    ap.add_argument("--omega", type=float, default=1.7)
+    ap.add_argument("--checkinterval", type=int, default=25)
+    ap.add_argument("--switch-eps", type=float, default=0.0)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
+    ap.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample sweeps (0: auto)")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def mt_params_path():
+    for p in (os.environ.get("GFX_MT_DAT"), os.path.join(os.getcwd(), "MersenneTwister.dat"),
+              os.path.join(ROOT, "oracle", "_ref", "MersenneTwister.dat")):
+        if p and os.path.exists(p):
+            return p
+    return None
+
+
+def synthetic_mt_params(seed=4172):
+    rng = np.random.default_rng(seed)
+    p = rng.integers(0, 2 ** 32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
+    p[:, 0] |= np.uint32(0x80000000)
+    p[:, 3] = 0
+    return p
+
+
+# ---------------------------------------------------------------------------
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        import torch
+        t = torch.zeros(1, device="cuda")
+        dist.all_reduce(t)
+        torch.cuda.synchronize()
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_rate(dims, sweeps, omega, seed=351):
+    """CPU port of the reference's OR update, all host threads, `sweeps` sweeps."""
+    import oracle as orc
+    o = orc.Oracle()
+    lat = o.lattice(dims)
+    V = int(np.prod(dims))
+    rng = np.random.default_rng(seed)
+    # near-identity links and the reference's random gauge start
+    z = rng.normal(size=(4 * V, 12)) * 0.3
+    gf = np.zeros((4 * V, 12))
+    gf[:, 0] = 1.0
+    gf[:, 8] = 1.0
+    gf += z
+    # rows 0,1 orthonormalized (row 2 is reconstructed by the update)
+    r0 = gf[:, 0:6:2] + 1j * gf[:, 1:6:2]
+    r1 = gf[:, 6:12:2] + 1j * gf[:, 7:12:2]
+    r0 /= np.linalg.norm(r0, axis=1, keepdims=True)
+    r1 = r1 - np.sum(r1 * np.conj(r0), axis=1, keepdims=True) * r0
+    r1 /= np.linalg.norm(r1, axis=1, keepdims=True)
+    gf[:, 0:6:2], gf[:, 1:6:2], gf[:, 6:12:2], gf[:, 7:12:2] = r0.real, r0.imag, r1.real, r1.imag
+    pm = o.pm_new(seed)
+    g = np.ascontiguousarray(o.random_init(pm, V)[:, :12])
+    o.or_halfsweep(lat, gf, g, 0, omega)  # warm the threads
+    t0 = time.perf_counter()
+    o.or_sweeps(lat, gf, g, sweeps, omega)
+    dt = time.perf_counter() - t0
+    return sweeps * V / dt, dt, os.cpu_count()
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, dims):
+    rank, ws, local, dist = dist_init(args)
+    if rank != 0:
+        return
+    V = int(np.prod(dims))
+    sweeps = args.cpu_sweeps or 2
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_reference_rate(dims, 1, args.omega)
+    rates, tot = [], 0.0
+    for _ in range(args.steps):
+        r, dt, cores = cpu_reference_rate(dims, sweeps, args.omega)
+        rates.append(r)
+        tot += dt
+    value = float(np.mean(rates))
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "%s Landau OR half-sweeps (omega=%g), CPU restatement of the "
+                               "reference update, all host threads" % ("x".join(map(str, dims)),
+                                                                       args.omega),
+                   "lattice": list(dims), "sweeps_per_step": sweeps},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": "%d OR sweeps of %s per step, OpenMP over one parity"
+                                   % (sweeps, "x".join(map(str, dims)))},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def run_gfx(args, dims):
+    rank, ws, local, dist = dist_init(args)
+    from cudagfx_gb300 import build as b
+    if rank == 0:
+        b.build()
+    barrier(dist)
+    import cudagfx_gb300 as gfx
+
+    V = int(np.prod(dims))
+    # ---- inputs: heatbath links (beta, cold start), reference random gauge start
+    ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    ctx.set_links(gfx.unit_init(4 * V))
+    dat = mt_params_path()
+    if dat:
+        ctx.mt_load_file(dat)
+    else:
+        ctx.mt_load_params(synthetic_mt_params())
+    ctx.mt_seed(42 + rank)
+    ctx.mt_init(2 * V, 8 * V)
+    t0 = time.perf_counter()
+    ctx.thermalize(args.beta, args.therm)
+    therm_s = time.perf_counter() - t0
+    plaq = ctx.plaquette()
+    links = ctx.get_links()
+    g0 = gfx.random_init_reference(351 + rank, V)
+    params = ctx.or_params(maxit=200000, eps=args.eps, checkinterval=args.checkinterval,
+                           omega=args.omega, criterion=gfx.CRIT_THETA,
+                           switch_eps=args.switch_eps, checkinterval_double=args.checkinterval)
+
+    def solve(c):
+        c.set_trafo(g0)
+        r = c.overrelax(params)
+        if not r.converged:
+            raise RuntimeError("did not converge: %d sweeps" % r.sweeps)
+        return r
+
+    for _ in range(args.warmup):
+        solve(ctx)
+    # ---- timed region: K solves, device time of each (CUDA events on the ctx stream)
+    barrier(dist)
+    launches0 = ctx.launch_count()
+    with ClockSampler(local) as clk:
+        results = [solve(ctx) for _ in range(args.steps)]
+    launches = ctx.launch_count() - launches0
+    ms_total = sum(r.ms for r in results)
+    ms_total = max_over_ranks(dist, ms_total)
+    updates = sum(r.sweeps for r in results) * V
+    value = updates * ws / (ms_total / 1000.0)
+    r_last = results[-1]
+    clocks = clk.summary()
+
+    # ---- e2e through the public API with pinned host buffers
+    pin_links = gfx.pinned_empty(links.shape)
+    pin_links[...] = links
+    pin_g0 = gfx.pinned_empty(g0.shape)
+    pin_g0[...] = g0
+    pin_out = gfx.pinned_empty(g0.shape)
+    e2e_t, e2e_upd = 0.0, 0
+    for _ in range(args.steps):
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_links(pin_links)
+        ctx.set_trafo(pin_g0)
+        r = ctx.overrelax(params)
+        ctx.get_trafo_into(pin_out)
+        e2e_t += time.perf_counter() - t0
+        e2e_upd += r.sweeps * V
+    e2e_t = max_over_ranks(dist, e2e_t)
+    e2e_value = e2e_upd * ws / e2e_t
+
+    # ---- kernel timing for the roofline (FP32 and FP64 half-sweeps)
+    ctx.set_trafo(g0)
+    nt = 20
+    ms32 = ctx.time_sweeps(nt, args.omega, precision=0) / (2 * nt)
+    ms64 = None
+    t_fp64 = None
+    sweeps64 = None
+    if not args.no_fp64:
+        c64 = gfx.Context(dims, precision=gfx.PREC_DOUBLE)
+        c64.set_links(links)
+        c64.set_trafo(g0)
+        ms64 = c64.time_sweeps(4, args.omega, precision=1) / 8
+        r64 = solve(c64)
+        t_fp64 = r64.ms / 1000.0
+        sweeps64 = r64.sweeps
+        c64.close()
+    hbm, peak_kind = measured_peaks()
+    t32_share = r_last.sweeps_single * 2 * ms32
+    t64_share = r_last.sweeps_double * 2 * (ms64 if ms64 else 0.0)
+    bytes32 = BYTES_PER_UPDATE_FP32 * V / 2
+    ach32 = bytes32 / (ms32 / 1000.0) / 1e9
+    roof = {"bound": "hbm", "kernel": "or_halfsweep_kernel<float,12,4>",
+            "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
+            "peak_source": peak_kind,
+            "traffic": NCU_TRAFFIC_FP32, "ms_per_launch": ms32,
+            "bytes_per_launch": bytes32,
+            "time_share_in_solve": t32_share / max(r_last.ms, 1e-9)}
+    if ms64:
+        roof["fp64_kernel"] = {"kernel": "or_halfsweep_kernel<double,12,4>", "ms_per_launch": ms64,
+                               "gflops": FLOP_PER_UPDATE * V / 2 / (ms64 / 1000.0) / 1e9,
+                               "time_share_in_solve": t64_share / max(r_last.ms, 1e-9)}
+
+    cpu = None
+    if rank == 0:
+        cs = args.cpu_sweeps or 2
+        rate, dt, cores = cpu_reference_rate(dims, cs, args.omega)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d OR sweeps of %s (%.1f s), CPU restatement of the reference update, "
+                         "OpenMP over one parity" % (cs, "x".join(map(str, dims)), dt)}
+    ctx.close()
+    if rank != 0:
+        return
+    h2d = pin_links.nbytes + pin_g0.nbytes
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {
+            "workload": "%s Landau gauge fixing: beta=%g heatbath links (%d sweeps from cold, MT "
+                        "seed 42), reference random gauge start (RandSeed 351), mixed FP32->FP64 "
+                        "OR omega=%g to theta<%g" % ("x".join(map(str, dims)), args.beta,
+                                                     args.therm, args.omega, args.eps),
+            "lattice": list(dims), "omega": args.omega, "eps": args.eps, "criterion": "theta",
+            "checkinterval": args.checkinterval, "parallelism": "replicas" if ws > 1 else "1 GPU",
+            "l2": "inputs larger than L2 (FP32 links %d MB, FP64 links %d MB)"
+                  % (V * 4 * 48 // 2 ** 20, V * 4 * 96 // 2 ** 20),
+            "mt_params": "reference file" if dat else "synthetic stand-in",
+            "plaquette": plaq, "therm_s": therm_s},
+        "sweeps_per_solve": {"total": r_last.sweeps, "fp32": r_last.sweeps_single,
+                             "fp64": r_last.sweeps_double},
+        "time_to_theta_s": {"mixed": r_last.ms / 1000.0, "fp64": t_fp64,
+                            "fp64_sweeps": sweeps64,
+                            "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": pin_out.nbytes},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    dims = tuple(int(x) for x in args.dims.split(","))
+    if args.impl == "reference":
+        run_reference(args, dims)
+    else:
+        run_gfx(args, dims)
+
+
+if __name__ == "__main__":
+    main()

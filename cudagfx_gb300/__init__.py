@@ -1,0 +1,417 @@
+"""cudagfx_gb300 -- Python host mirror of the cudagfx gauge-fixing interface on GB300.
+
+Everything here calls libgfx.so (the sm_103a CUDA library, C ABI in include/gfx.h)
+through ctypes.  There is no CPU fallback: importing the package raises when the
+library has not been built (``cudagfx_gb300.build.build()``).
+
+Two layers, as in the C ABI:
+  * ``Context``: one lattice on the GPU with explicit-argument methods
+    (set_links, overrelax, functional, plaquette, polyakov, simanneal, thermalize,
+    the twister bank ...);
+  * reference-named functions (``init_gaugefixing``, ``overrelax_gauge``,
+    ``calc_functional``, ``calc_plaquette``, ``simannealing_gauge``,
+    ``thermalize_gauge``, ``init_MT``, ``update_MT``) acting on the library's
+    process-wide context and the reference's globals (``globals_()``).
+
+Host arrays are numpy float64 arrays of shape (n, 3, 3, 2) or any shape with
+18 doubles per SU(3) matrix, ordered as the reference's su3 (complex[3][3]).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["lib", "Context", "GfxError", "ORParams", "ORResult", "Functional", "SAParams",
+           "ThermParams", "PREC_DOUBLE", "PREC_SINGLE", "PREC_MIXED", "LANDAU", "COULOMB",
+           "CRIT_MAXDADA", "CRIT_THETA", "CRIT_THETA_SLICES", "glibc_rand",
+           "random_init_reference", "random_init_haar", "unit_init", "library_path"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libgfx.so")
+
+PREC_DOUBLE, PREC_SINGLE, PREC_MIXED = 0, 1, 2
+LANDAU, COULOMB = 0, 1
+CRIT_MAXDADA, CRIT_THETA, CRIT_THETA_SLICES = 0, 1, 2
+STATUS = {0: "GFX_OK", 1: "GFX_ERR_BAD_VOLUME", 2: "GFX_ERR_OOM", 3: "GFX_ERR_NOT_CONVERGED",
+          4: "GFX_ERR_IO", 5: "GFX_ERR_CUDA", 6: "GFX_ERR_ARG", 7: "GFX_ERR_STATE"}
+
+
+def library_path():
+    return _LIB_PATH
+
+
+if not os.path.exists(_LIB_PATH):
+    raise ImportError("cudagfx_gb300: %s is missing; build it with "
+                      "`python -m cudagfx_gb300.build` (nvcc, sm_103a)" % _LIB_PATH)
+
+# RTLD_LOCAL: libgfx defines the reference's globals (LX, VOLUME, FUNC, ...); keep them
+# out of the global namespace so other libraries in the process keep their own.
+lib = ctypes.CDLL(_LIB_PATH, mode=ctypes.RTLD_LOCAL)
+
+_c = ctypes
+_dp = _c.POINTER(_c.c_double)
+_fp = _c.POINTER(_c.c_float)
+_u32p = _c.POINTER(_c.c_uint32)
+_i32p = _c.POINTER(_c.c_int32)
+
+
+class Functional(_c.Structure):
+    _fields_ = [("F", _c.c_double), ("dAdA", _c.c_double), ("maxdAdA", _c.c_double),
+                ("theta", _c.c_double), ("theta_slice_max", _c.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ORParams(_c.Structure):
+    _fields_ = [("maxit", _c.c_int), ("eps", _c.c_double), ("checkinterval", _c.c_int),
+                ("omega", _c.c_double), ("criterion", _c.c_int), ("gauge", _c.c_int),
+                ("switch_eps", _c.c_double), ("plateau_ratio", _c.c_double),
+                ("checkinterval_double", _c.c_int), ("use_graph", _c.c_int),
+                ("record_history", _c.c_int)]
+
+
+class ORResult(_c.Structure):
+    _fields_ = [("iterations", _c.c_int), ("sweeps", _c.c_int), ("sweeps_single", _c.c_int),
+                ("sweeps_double", _c.c_int), ("converged", _c.c_int), ("checks", _c.c_int),
+                ("final_values", Functional), ("ms", _c.c_double)]
+
+
+class CheckRecord(_c.Structure):
+    _fields_ = [("iter", _c.c_int), ("phase", _c.c_int), ("F", _c.c_double),
+                ("dAdA", _c.c_double), ("maxdAdA", _c.c_double), ("theta", _c.c_double),
+                ("theta_slice_max", _c.c_double)]
+
+
+class SAParams(_c.Structure):
+    _fields_ = [("Tmin", _c.c_double), ("Tmax", _c.c_double), ("expo", _c.c_double),
+                ("N", _c.c_int), ("checkint", _c.c_int), ("nmicro", _c.c_int)]
+
+
+class ThermParams(_c.Structure):
+    _fields_ = [("Nsweep", _c.c_int), ("checkint", _c.c_int), ("beta", _c.c_double)]
+
+
+def _sig(name, res, args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = args
+    return f
+
+
+_V = _c.c_void_p
+_I = _c.c_int
+_D = _c.c_double
+_sig("gfx_abi_version", _I, [])
+_sig("gfx_status_string", _c.c_char_p, [_I])
+_sig("gfx_last_error", _c.c_char_p, [_V])
+_sig("gfx_create", _I, [_c.POINTER(_V), _I, _I, _I, _I, _I, _I, _V])
+_sig("gfx_destroy", _I, [_V])
+_sig("gfx_synchronize", _I, [_V])
+_sig("gfx_device_bytes", _c.c_size_t, [_V])
+_sig("gfx_set_block", _I, [_V, _I])
+for _n in ("gfx_set_links", "gfx_get_links", "gfx_set_trafo", "gfx_get_trafo"):
+    _sig(_n, _I, [_V, _dp])
+_sig("gfx_unit_trafo", _I, [_V])
+_sig("gfx_or_params_default", None, [_c.POINTER(ORParams)])
+_sig("gfx_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(ORResult)])
+_sig("gfx_or_history", _I, [_V, _c.POINTER(CheckRecord), _I])
+_sig("gfx_or_sweeps", _I, [_V, _I, _D, _I, _I])
+_sig("gfx_or_halfsweep", _I, [_V, _I, _D, _I, _I])
+_sig("gfx_functional", _I, [_V, _I, _I, _c.POINTER(Functional)])
+_sig("gfx_plaquette", _I, [_V, _dp])
+_sig("gfx_polyakov", _I, [_V, _dp])
+_sig("gfx_apply_trafo", _I, [_V])
+_sig("gfx_mt_load_params", _I, [_V, _u32p])
+_sig("gfx_mt_load_file", _I, [_V, _c.c_char_p])
+_sig("gfx_mt_seed", _I, [_V, _c.c_uint])
+_sig("gfx_mt_set_seeds", _I, [_V, _u32p])
+_sig("gfx_mt_init", _I, [_V, _I, _I])
+_sig("gfx_mt_update", _I, [_V])
+_sig("gfx_mt_read", _I, [_V, _fp, _fp, _u32p, _u32p])
+_sig("gfx_mt_sizes", _I, [_V, _c.POINTER(_I), _c.POINTER(_I)])
+_sig("gfx_sa_temperature", _D, [_c.POINTER(SAParams), _I])
+_sig("gfx_simanneal", _I, [_V, _c.POINTER(SAParams), _c.POINTER(Functional)])
+_sig("gfx_simanneal_range", _I, [_V, _c.POINTER(SAParams), _I, _I])
+_sig("gfx_sa_halfsweep", _I, [_V, _I, _D, _I])
+_sig("gfx_micro_halfsweep", _I, [_V, _I, _I, _I])
+_sig("gfx_thermalize", _I, [_V, _c.POINTER(ThermParams), _dp, _I])
+_sig("gfx_link_heatbath_halfsweep", _I, [_V, _I, _I, _D])
+_sig("gfx_time_sweeps", _I, [_V, _I, _D, _I, _I, _dp])
+_sig("gfx_launch_count", _c.c_ulonglong, [_V])
+_sig("gfx_glibc_rand", None, [_c.c_uint, _I, _i32p])
+_sig("gfx_random_init_reference", None, [_c.c_long, _dp, _c.c_long])
+_sig("gfx_random_init_haar", None, [_c.c_uint64, _dp, _c.c_long])
+_sig("gfx_unit_init", None, [_dp, _c.c_long])
+
+
+class GfxError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+def _ptr(a, ctype=_c.c_double):
+    return a.ctypes.data_as(_c.POINTER(ctype))
+
+
+def _f64(a, n):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.size != 18 * n:
+        raise ValueError("expected %d SU(3) matrices (%d doubles), got %d doubles"
+                         % (n, 18 * n, a.size))
+    return a
+
+
+_sig("gfx_host_alloc", _V, [_c.c_size_t])
+_sig("gfx_host_free", None, [_V])
+
+
+class _Pinned:
+    def __init__(self, nbytes):
+        self.ptr = lib.gfx_host_alloc(nbytes)
+        if not self.ptr:
+            raise MemoryError("cudaMallocHost(%d) failed" % nbytes)
+
+    def __del__(self):
+        if self.ptr:
+            lib.gfx_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float64):
+    """numpy array in page-locked host memory (freed with the array)."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    keep = _Pinned(max(n, 1))
+    buf = (_c.c_char * n).from_address(keep.ptr)
+    buf._owner = keep  # the array's base chain keeps buf, buf keeps the allocation
+    return np.frombuffer(buf, dtype=dtype).reshape(shape)
+
+
+def glibc_rand(seed, n):
+    out = np.empty(n, dtype=np.int32)
+    lib.gfx_glibc_rand(seed, n, _ptr(out, _c.c_int32))
+    return out
+
+
+def random_init_reference(seed, n):
+    """random_init_trafo / random_init_gauge after PlantSeeds(seed) (n matrices)."""
+    out = np.empty((n, 3, 3, 2))
+    lib.gfx_random_init_reference(seed, _ptr(out), n)
+    return out
+
+
+def random_init_haar(seed, n):
+    out = np.empty((n, 3, 3, 2))
+    lib.gfx_random_init_haar(seed, _ptr(out), n)
+    return out
+
+
+def unit_init(n):
+    out = np.empty((n, 3, 3, 2))
+    lib.gfx_unit_init(_ptr(out), n)
+    return out
+
+
+class Context:
+    """One lattice on the current CUDA device (gfx_create)."""
+
+    def __init__(self, dims, precision=PREC_DOUBLE, link_reals=12, stream=None):
+        lx, ly, lz, lt = dims
+        h = _V()
+        s = lib.gfx_create(_c.byref(h), lx, ly, lz, lt, precision, link_reals,
+                           _V(stream) if stream else None)
+        if s != 0:
+            raise GfxError(s, lib.gfx_last_error(None).decode())
+        self._h = h
+        self.dims = (lx, ly, lz, lt)
+        self.volume = lx * ly * lz * lt
+        self.precision = precision
+
+    def _check(self, s, ok=(0,)):
+        if s not in ok:
+            raise GfxError(s, lib.gfx_last_error(self._h).decode())
+        return s
+
+    def close(self):
+        if self._h:
+            lib.gfx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def device_bytes(self):
+        return lib.gfx_device_bytes(self._h)
+
+    def set_block(self, b):
+        self._check(lib.gfx_set_block(self._h, b))
+
+    def synchronize(self):
+        self._check(lib.gfx_synchronize(self._h))
+
+    # ---- fields
+    def set_links(self, u):
+        u = _f64(u, 4 * self.volume)
+        self._check(lib.gfx_set_links(self._h, _ptr(u)))
+
+    def get_links(self):
+        out = np.empty((4 * self.volume, 3, 3, 2))
+        self._check(lib.gfx_get_links(self._h, _ptr(out)))
+        return out
+
+    def set_trafo(self, g):
+        g = _f64(g, self.volume)
+        self._check(lib.gfx_set_trafo(self._h, _ptr(g)))
+
+    def get_trafo(self):
+        out = np.empty((self.volume, 3, 3, 2))
+        self._check(lib.gfx_get_trafo(self._h, _ptr(out)))
+        return out
+
+    def get_trafo_into(self, out):
+        if out.dtype != np.float64 or out.size != 18 * self.volume or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of V su3 matrices")
+        self._check(lib.gfx_get_trafo(self._h, _ptr(out)))
+        return out
+
+    def unit_trafo(self):
+        self._check(lib.gfx_unit_trafo(self._h))
+
+    # ---- gauge fixing
+    @staticmethod
+    def or_params(**kw):
+        p = ORParams()
+        lib.gfx_or_params_default(_c.byref(p))
+        for k, v in kw.items():
+            if not hasattr(p, k):
+                raise AttributeError(k)
+            setattr(p, k, v)
+        return p
+
+    def overrelax(self, params=None, **kw):
+        p = params if params is not None else self.or_params(**kw)
+        r = ORResult()
+        self._check(lib.gfx_overrelax(self._h, _c.byref(p), _c.byref(r)), ok=(0, 3))
+        return r
+
+    def history(self):
+        n = lib.gfx_or_history(self._h, None, 0)
+        arr = (CheckRecord * max(n, 1))()
+        lib.gfx_or_history(self._h, arr, n)
+        return [{k: getattr(arr[i], k) for k, _ in CheckRecord._fields_} for i in range(n)]
+
+    def or_sweeps(self, n, omega=1.68, gauge=LANDAU, precision=1):
+        self._check(lib.gfx_or_sweeps(self._h, n, omega, gauge, precision))
+
+    def time_sweeps(self, n, omega=1.68, gauge=LANDAU, precision=1):
+        ms = np.zeros(1)
+        self._check(lib.gfx_time_sweeps(self._h, n, omega, gauge, precision, _ptr(ms)))
+        return float(ms[0])
+
+    def launch_count(self):
+        return lib.gfx_launch_count(self._h)
+
+    def or_halfsweep(self, parity, omega=1.68, gauge=LANDAU, precision=1):
+        self._check(lib.gfx_or_halfsweep(self._h, parity, omega, gauge, precision))
+
+    def functional(self, gauge=LANDAU, precision=1):
+        f = Functional()
+        self._check(lib.gfx_functional(self._h, gauge, precision, _c.byref(f)))
+        return f
+
+    def plaquette(self):
+        v = np.zeros(1)
+        self._check(lib.gfx_plaquette(self._h, _ptr(v)))
+        return float(v[0])
+
+    def polyakov(self):
+        v = np.zeros(2)
+        self._check(lib.gfx_polyakov(self._h, _ptr(v)))
+        return complex(v[0], v[1])
+
+    def apply_trafo(self):
+        self._check(lib.gfx_apply_trafo(self._h))
+
+    # ---- twister bank
+    def mt_load_params(self, params):
+        p = np.ascontiguousarray(params, dtype=np.uint32).reshape(-1)
+        if p.size != 4 * 4096:
+            raise ValueError("twister parameters: 4096 x {matrix_a, mask_b, mask_c, seed}")
+        self._check(lib.gfx_mt_load_params(self._h, _ptr(p, _c.c_uint32)))
+
+    def mt_load_file(self, path):
+        self._check(lib.gfx_mt_load_file(self._h, os.fsencode(path)))
+
+    def mt_seed(self, seed):
+        self._check(lib.gfx_mt_seed(self._h, seed))
+
+    def mt_set_seeds(self, seeds):
+        s = np.ascontiguousarray(seeds, dtype=np.uint32)
+        self._check(lib.gfx_mt_set_seeds(self._h, _ptr(s, _c.c_uint32)))
+
+    def mt_init(self, n_gauss, n_unif):
+        self._check(lib.gfx_mt_init(self._h, n_gauss, n_unif))
+
+    def mt_update(self):
+        self._check(lib.gfx_mt_update(self._h))
+
+    def mt_sizes(self):
+        a, b = _I(), _I()
+        lib.gfx_mt_sizes(self._h, _c.byref(a), _c.byref(b))
+        return a.value, b.value
+
+    def mt_read(self):
+        ng, nu = self.mt_sizes()
+        g = np.empty(4096 * ng, dtype=np.float32)
+        u = np.empty(4096 * nu, dtype=np.float32)
+        st = np.empty(19 * 4096, dtype=np.uint32)
+        sd = np.empty(4096, dtype=np.uint32)
+        self._check(lib.gfx_mt_read(self._h, _ptr(g, _c.c_float), _ptr(u, _c.c_float),
+                                    _ptr(st, _c.c_uint32), _ptr(sd, _c.c_uint32)))
+        return g, u, st.reshape(19, 4096), sd
+
+    # ---- simulated annealing / thermalization
+    def simanneal(self, Tmin, Tmax, N, expo=-1.0, checkint=100, nmicro=0):
+        p = SAParams(Tmin, Tmax, expo, N, checkint, nmicro)
+        f = Functional()
+        self._check(lib.gfx_simanneal(self._h, _c.byref(p), _c.byref(f)))
+        return f
+
+    def sa_halfsweep(self, parity, beta, precision=1):
+        self._check(lib.gfx_sa_halfsweep(self._h, parity, beta, precision))
+
+    def micro_halfsweep(self, parity, gauge=LANDAU, precision=1):
+        self._check(lib.gfx_micro_halfsweep(self._h, parity, gauge, precision))
+
+    def thermalize(self, beta, nsweep, checkint=0):
+        p = ThermParams(nsweep, checkint, beta)
+        cap = nsweep // checkint + 1 if checkint > 0 else 0
+        plaq = np.zeros(max(cap, 1))
+        self._check(lib.gfx_thermalize(self._h, _c.byref(p), _ptr(plaq), cap))
+        return plaq[:cap]
+
+    def link_heatbath_halfsweep(self, parity, nu, beta):
+        self._check(lib.gfx_link_heatbath_halfsweep(self._h, parity, nu, beta))
+
+
+def sa_temperature(Tmin, Tmax, N, expo, i):
+    p = SAParams(Tmin, Tmax, expo, N, 1, 0)
+    return lib.gfx_sa_temperature(_c.byref(p), i)
+
+
+from . import legacy  # noqa: E402,F401  (reference-named entry points)

@@ -1,0 +1,1040 @@
+// gfx_api.cu -- contexts, buffers and drivers behind the gfx_* C ABI.
+//
+// One context = one lattice on the current device, with
+//   U64 : links, FP64, 12 or 18 reals, even/odd SoA (authoritative copy)
+//   G64 : gauge transformation, FP64, 12 reals
+//   U32, G32 : FP32 12-real copies for the single/mixed-precision sweeps
+// and the work buffers of the reductions, the convergence loop and the twister bank.
+// Everything runs on the context's stream; host synchronisation happens only where
+// a result is returned to the caller.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <string>
+#include <vector>
+
+#include "../../include/gfx.h"
+#include "gfx_internal.h"
+
+using namespace gfx;
+
+struct gfx_ctx {
+  int lx, ly, lz, lt;
+  long long vol;
+  Lattice L;
+  int precision;
+  int link_nr;  // FP64 link storage: 12 or 18
+  int block;
+  cudaStream_t stream;
+  bool own_stream;
+  int g_active;  // 0: G32 holds the current g, 1: G64 does
+  // fields
+  void* U64;
+  void* G64;
+  void* U32;
+  void* G32;
+  // reductions
+  double* partials;
+  int part_cap;  // doubles
+  double* slice_sums;
+  Reduced* reduced;
+  LoopState* loop;
+  CheckRecord* hist;
+  int hist_cap;
+  LoopState* loop_host;  // pinned
+  Reduced* reduced_host; // pinned
+  double* scratch_aos;   // device staging for host<->device layout conversion
+  size_t scratch_bytes;
+  // twister bank
+  MTBank bank;
+  bool mt_params;
+  bool mt_seeded;
+  bool mt_init;
+  int n_gauss, n_unif, nper_g, nper_u;
+  float* gauss;
+  float* unif;
+  uint32_t h_params[4 * kMTCount];
+  // graph cache for the convergence loop
+  struct GraphEntry {
+    int cprec, ndir, ck, gprec;
+    double omega;
+    cudaGraphExec_t exec;
+    cudaGraph_t graph;
+  };
+  std::vector<GraphEntry> graphs;
+  std::vector<CheckRecord> last_hist;
+  size_t dev_bytes;
+  unsigned long long launches;  // kernels enqueued by this context (graph bodies included)
+  std::string err;
+};
+
+static std::string g_global_err;
+
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      return fail(ctx, GFX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                                \
+  } while (0)
+
+static gfx_status fail(gfx_ctx* ctx, gfx_status s, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  g_global_err = msg;
+  return s;
+}
+
+static gfx_status dalloc(gfx_ctx* ctx, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? GFX_ERR_OOM : GFX_ERR_CUDA,
+                std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+  }
+  ctx->dev_bytes += bytes;
+  return GFX_OK;
+}
+
+static size_t link_bytes64(const gfx_ctx* c) {
+  return (size_t)8 * (c->link_nr / 2) * 16 * (size_t)c->L.vh;  // 8 blocks x chunks x 16 B
+}
+static size_t link_bytes32(const gfx_ctx* c) { return (size_t)8 * 3 * 16 * (size_t)c->L.vh; }
+static size_t g_bytes64(const gfx_ctx* c) { return (size_t)2 * 6 * 16 * (size_t)c->L.vh; }
+static size_t g_bytes32(const gfx_ctx* c) { return (size_t)2 * 3 * 16 * (size_t)c->L.vh; }
+
+static gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes) {
+  if (ctx->scratch_bytes >= bytes) return GFX_OK;
+  if (ctx->scratch_aos) {
+    cudaFree(ctx->scratch_aos);
+    ctx->dev_bytes -= ctx->scratch_bytes;
+    ctx->scratch_aos = nullptr;
+    ctx->scratch_bytes = 0;
+  }
+  gfx_status s = dalloc(ctx, (void**)&ctx->scratch_aos, bytes);
+  if (s == GFX_OK) ctx->scratch_bytes = bytes;
+  return s;
+}
+
+static gfx_status ensure_hist(gfx_ctx* ctx, int cap) {
+  if (ctx->hist_cap >= cap) return GFX_OK;
+  if (ctx->hist) {
+    cudaFree(ctx->hist);
+    ctx->dev_bytes -= sizeof(CheckRecord) * ctx->hist_cap;
+  }
+  ctx->hist = nullptr;
+  ctx->hist_cap = 0;
+  gfx_status s = dalloc(ctx, (void**)&ctx->hist, sizeof(CheckRecord) * (size_t)cap);
+  if (s == GFX_OK) ctx->hist_cap = cap;
+  return s;
+}
+
+extern "C" {
+
+const char* gfx_last_error(const gfx_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_global_err.c_str();
+}
+
+static void destroy_graphs(gfx_ctx* ctx) {
+  for (auto& g : ctx->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  ctx->graphs.clear();
+}
+
+gfx_status gfx_destroy(gfx_ctx* ctx) {
+  if (!ctx) return GFX_OK;
+  cudaStreamSynchronize(ctx->stream);
+  destroy_graphs(ctx);
+  void* ptrs[] = {ctx->U64,     ctx->G64,  ctx->U32,  ctx->G32,  ctx->partials,
+                  ctx->slice_sums, ctx->reduced, ctx->loop, ctx->hist, ctx->scratch_aos,
+                  ctx->bank.a,  ctx->bank.b, ctx->bank.c, ctx->bank.seed, ctx->bank.status,
+                  ctx->gauss,   ctx->unif};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (ctx->loop_host) cudaFreeHost(ctx->loop_host);
+  if (ctx->reduced_host) cudaFreeHost(ctx->reduced_host);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GFX_OK;
+}
+
+gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precision,
+                      int link_reals64, void* stream) {
+  gfx_ctx* ctx = nullptr;
+  if (!out) return fail(nullptr, GFX_ERR_ARG, "gfx_create: out is NULL");
+  *out = nullptr;
+  if (lx < 2 || ly < 2 || lz < 2 || lt < 2 || (lx | ly | lz | lt) & 1)
+    return fail(nullptr, GFX_ERR_BAD_VOLUME, "gfx_create: every extent must be even and >= 2");
+  const long long vol = (long long)lx * ly * lz * lt;
+  if (vol / 2 > (1ll << 30))
+    return fail(nullptr, GFX_ERR_BAD_VOLUME, "gfx_create: volume/2 must be below 2^30 sites");
+  if (precision < GFX_PREC_DOUBLE || precision > GFX_PREC_MIXED)
+    return fail(nullptr, GFX_ERR_ARG, "gfx_create: unknown precision");
+  if (link_reals64 == 0) link_reals64 = 12;
+  if (link_reals64 != 12 && link_reals64 != 18)
+    return fail(nullptr, GFX_ERR_ARG, "gfx_create: link_reals64 must be 12 or 18");
+  ctx = new gfx_ctx();
+  std::memset((void*)&ctx->bank, 0, sizeof(ctx->bank));
+  ctx->lx = lx;
+  ctx->ly = ly;
+  ctx->lz = lz;
+  ctx->lt = lt;
+  ctx->vol = vol;
+  ctx->L = make_lattice(lx, ly, lz, lt);
+  ctx->precision = precision;
+  ctx->link_nr = link_reals64;
+  ctx->block = 128;
+  ctx->g_active = 1;
+  ctx->U64 = ctx->G64 = ctx->U32 = ctx->G32 = nullptr;
+  ctx->partials = ctx->slice_sums = nullptr;
+  ctx->reduced = nullptr;
+  ctx->loop = nullptr;
+  ctx->hist = nullptr;
+  ctx->hist_cap = 0;
+  ctx->loop_host = nullptr;
+  ctx->reduced_host = nullptr;
+  ctx->scratch_aos = nullptr;
+  ctx->scratch_bytes = 0;
+  ctx->mt_params = ctx->mt_seeded = ctx->mt_init = false;
+  ctx->gauss = ctx->unif = nullptr;
+  ctx->dev_bytes = 0;
+  ctx->launches = 0;
+  gfx_status s;
+  if (stream) {
+    ctx->stream = (cudaStream_t)stream;
+    ctx->own_stream = false;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete ctx;
+      return fail(nullptr, GFX_ERR_CUDA, std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    }
+    ctx->own_stream = true;
+  }
+#define TRY(x)           \
+  do {                   \
+    s = (x);             \
+    if (s != GFX_OK) {   \
+      std::string m = ctx->err; \
+      gfx_destroy(ctx);  \
+      g_global_err = m;  \
+      return s;          \
+    }                    \
+  } while (0)
+  TRY(dalloc(ctx, &ctx->U64, link_bytes64(ctx)));
+  TRY(dalloc(ctx, &ctx->G64, g_bytes64(ctx)));
+  if (precision != GFX_PREC_DOUBLE) {
+    TRY(dalloc(ctx, &ctx->U32, link_bytes32(ctx)));
+    TRY(dalloc(ctx, &ctx->G32, g_bytes32(ctx)));
+  }
+  // measurement partials: 3 doubles per block, blocks of >= 64 threads
+  const int nbx = measure_blocks_x(ctx->L, 64);
+  ctx->part_cap = 3 * 2 * lt * nbx;
+  const int plaq_blocks = 2 * ((ctx->L.vh + 127) / 128);
+  const int v3 = lx * ly * lz;
+  if (3 * plaq_blocks > ctx->part_cap) ctx->part_cap = 3 * plaq_blocks;
+  if (3 * ((v3 + 127) / 128) > ctx->part_cap) ctx->part_cap = 3 * ((v3 + 127) / 128);
+  TRY(dalloc(ctx, (void**)&ctx->partials, sizeof(double) * (size_t)ctx->part_cap));
+  TRY(dalloc(ctx, (void**)&ctx->slice_sums, sizeof(double) * 3 * (size_t)lt));
+  TRY(dalloc(ctx, (void**)&ctx->reduced, sizeof(Reduced)));
+  TRY(dalloc(ctx, (void**)&ctx->loop, sizeof(LoopState)));
+  {
+    cudaError_t e1 = cudaMallocHost((void**)&ctx->loop_host, sizeof(LoopState));
+    cudaError_t e2 = cudaMallocHost((void**)&ctx->reduced_host, sizeof(Reduced));
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      gfx_destroy(ctx);
+      return fail(nullptr, GFX_ERR_OOM, "cudaMallocHost failed");
+    }
+  }
+  TRY(ensure_hist(ctx, 64));
+#undef TRY
+  *out = ctx;
+  gfx_status r = gfx_unit_trafo(ctx);
+  if (r != GFX_OK) {
+    gfx_destroy(ctx);
+    *out = nullptr;
+    return r;
+  }
+  return GFX_OK;
+}
+
+gfx_status gfx_synchronize(gfx_ctx* ctx) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+size_t gfx_device_bytes(const gfx_ctx* ctx) { return ctx ? ctx->dev_bytes : 0; }
+
+gfx_status gfx_set_block(gfx_ctx* ctx, int block) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (block == 0) block = 128;
+  if (block < 32 || block > 256 || block % 32)
+    return fail(ctx, GFX_ERR_ARG, "block must be a multiple of 32 in [32, 256]");
+  ctx->block = block;
+  return GFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fields
+// ---------------------------------------------------------------------------
+gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
+  if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_set_links: NULL argument");
+  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  launch_pack_links(ctx->link_nr, ctx->L, ctx->scratch_aos, ctx->U64, ctx->stream);
+  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+static gfx_status sync_g64(gfx_ctx* ctx) {
+  if (ctx->g_active == 0) {
+    launch_convert_g(0, 1, ctx->L, ctx->G32, ctx->G64, ctx->stream);
+    CK(cudaGetLastError());
+    ctx->g_active = 1;
+  }
+  return GFX_OK;
+}
+
+gfx_status gfx_get_links(gfx_ctx* ctx, double* su3) {
+  if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_get_links: NULL argument");
+  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  launch_unpack_links(ctx->link_nr, ctx->L, ctx->U64, ctx->scratch_aos, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(su3, ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_set_trafo(gfx_ctx* ctx, const double* su3) {
+  if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_set_trafo: NULL argument");
+  const size_t bytes = sizeof(double) * 18 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  launch_pack_g(1, ctx->L, ctx->scratch_aos, ctx->G64, ctx->stream);
+  CK(cudaGetLastError());
+  ctx->g_active = 1;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_get_trafo(gfx_ctx* ctx, double* su3) {
+  if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_get_trafo: NULL argument");
+  const size_t bytes = sizeof(double) * 18 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  s = sync_g64(ctx);
+  if (s) return s;
+  launch_unpack_g(1, ctx->L, ctx->G64, ctx->scratch_aos, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(su3, ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_unit_trafo(gfx_ctx* ctx) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  std::vector<double> h(18 * (size_t)ctx->vol);
+  gfx_unit_init(h.data(), ctx->vol);
+  return gfx_set_trafo(ctx, h.data());
+}
+
+// ---------------------------------------------------------------------------
+// sweeps and measurements
+// ---------------------------------------------------------------------------
+static gfx_status prepare_g(gfx_ctx* ctx, int prec) {
+  if (prec == 0) {
+    if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "FP32 sweeps need a SINGLE or MIXED context");
+    if (ctx->g_active == 1) {
+      launch_convert_g(1, 0, ctx->L, ctx->G64, ctx->G32, ctx->stream);
+      CK(cudaGetLastError());
+      ctx->g_active = 0;
+    }
+  } else {
+    gfx_status s = sync_g64(ctx);
+    if (s) return s;
+  }
+  return GFX_OK;
+}
+
+static void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
+  const void* U = prec == 0 ? ctx->U32 : ctx->U64;
+  void* G = prec == 0 ? ctx->G32 : ctx->G64;
+  for (int p = 0; p < 2; p++)
+    launch_or_halfsweep(prec, ctx->link_nr, ndir, ctx->L, U, G, p, omega, ctx->block, ctx->stream);
+  ctx->launches += 2;
+}
+
+static int meas_block(const gfx_ctx* ctx) {
+  // a measurement block covers part of one time slice of one parity
+  return ctx->L.st >= 128 ? 128 : 64;
+}
+
+static void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
+  const int b = meas_block(ctx);
+  const void* U = cprec == 0 ? ctx->U32 : ctx->U64;
+  const void* G = gprec == 0 ? ctx->G32 : ctx->G64;
+  launch_measure(cprec, ctx->link_nr, gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
+  ctx->launches += 1;
+}
+
+static void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
+                           unsigned long long handle, int use_handle) {
+  const int nbx = measure_blocks_x(ctx->L, meas_block(ctx));
+  launch_reduce(ctx->L, ndir, ctx->partials, nbx, ctx->slice_sums, ctx->reduced,
+                with_loop ? ctx->loop : nullptr, with_loop ? ctx->hist : nullptr, advance, handle,
+                use_handle, ctx->stream);
+  ctx->launches += 2;
+}
+
+gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, int precision) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (parity < 0 || parity > 1) return fail(ctx, GFX_ERR_ARG, "parity must be 0 or 1");
+  const int prec = precision == 0 ? 0 : 1;
+  gfx_status s = prepare_g(ctx, prec);
+  if (s) return s;
+  const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  launch_or_halfsweep(prec, ctx->link_nr, ndir, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
+                      prec == 0 ? ctx->G32 : ctx->G64, parity, omega, ctx->block, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_or_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  const int prec = precision == 0 ? 0 : 1;
+  gfx_status s = prepare_g(ctx, prec);
+  if (s) return s;
+  const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  for (int k = 0; k < nsweeps; k++) enqueue_sweep(ctx, prec, ndir, omega);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_functional(gfx_ctx* ctx, int gauge, int precision, gfx_functional_t* out) {
+  if (!ctx || !out) return fail(ctx, GFX_ERR_ARG, "gfx_functional: NULL argument");
+  const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  int cprec = precision == 0 ? 0 : 1;
+  if (cprec == 0 && !ctx->U32) cprec = 1;
+  if (cprec == 0) {
+    gfx_status s = prepare_g(ctx, 0);
+    if (s) return s;
+  }
+  const int gprec = cprec == 0 ? 0 : ctx->g_active;
+  enqueue_measure(ctx, cprec, gprec, ndir);
+  enqueue_reduce(ctx, ndir, false, 0, 0, 0);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(ctx->reduced_host, ctx->reduced, sizeof(Reduced), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const Reduced& r = *ctx->reduced_host;
+  out->F = r.F;
+  out->dAdA = r.dAdA;
+  out->maxdAdA = r.maxdAdA;
+  out->theta = r.theta;
+  out->theta_slice_max = r.theta_slice_max;
+  return GFX_OK;
+}
+
+gfx_status gfx_plaquette(gfx_ctx* ctx, double* plaq) {
+  if (!ctx || !plaq) return fail(ctx, GFX_ERR_ARG, "gfx_plaquette: NULL argument");
+  launch_plaquette(ctx->link_nr, ctx->L, ctx->U64, ctx->partials, (double*)ctx->reduced,
+                   ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(plaq, ctx->reduced, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_polyakov(gfx_ctx* ctx, double* re_im) {
+  if (!ctx || !re_im) return fail(ctx, GFX_ERR_ARG, "gfx_polyakov: NULL argument");
+  launch_polyakov(ctx->link_nr, ctx->L, ctx->U64, ctx->partials, (double*)ctx->reduced,
+                  ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(re_im, ctx->reduced, 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_apply_trafo(gfx_ctx* ctx) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  gfx_status s = sync_g64(ctx);
+  if (s) return s;
+  launch_apply_trafo(ctx->link_nr, ctx->L, ctx->U64, ctx->G64, ctx->stream);
+  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  CK(cudaGetLastError());
+  return gfx_unit_trafo(ctx);
+}
+
+// ---------------------------------------------------------------------------
+// convergence loop (overrelax_gauge, overrelax.cu:677-823)
+// ---------------------------------------------------------------------------
+void gfx_or_params_default(gfx_or_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->maxit = 20000;
+  p->eps = 1e-14;
+  p->checkinterval = 50;
+  p->omega = 1.68;
+  p->criterion = GFX_CRIT_MAXDADA;
+  p->gauge = GFX_GAUGE_LANDAU;
+  p->switch_eps = 0.0;
+  p->plateau_ratio = 0.98;
+  p->checkinterval_double = 0;
+  p->use_graph = 1;
+  p->record_history = 1;
+}
+
+// body of the device-side loop: ck sweeps, measurement, reduction + check
+static void enqueue_body(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
+                         unsigned long long handle, int use_handle) {
+  for (int k = 0; k < ck; k++) enqueue_sweep(ctx, prec, ndir, omega);
+  enqueue_measure(ctx, prec, prec, ndir);
+  enqueue_reduce(ctx, ndir, true, ck, handle, use_handle);
+}
+
+static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
+                            cudaGraphExec_t* exec) {
+  for (auto& g : ctx->graphs)
+    if (g.cprec == prec && g.ndir == ndir && g.ck == ck && g.omega == omega) {
+      *exec = g.exec;
+      return GFX_OK;
+    }
+  cudaGraph_t graph;
+  CK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  CK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  enqueue_body(ctx, prec, ndir, ck, omega, (unsigned long long)handle, 1);
+  cudaGraph_t captured;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &captured);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return fail(ctx, GFX_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+  }
+  cudaGraphExec_t ex;
+  CK(cudaGraphInstantiate(&ex, graph, 0));
+  gfx_ctx::GraphEntry ge;
+  ge.cprec = prec;
+  ge.ndir = ndir;
+  ge.ck = ck;
+  ge.gprec = prec;
+  ge.omega = omega;
+  ge.exec = ex;
+  ge.graph = graph;
+  ctx->graphs.push_back(ge);
+  *exec = ex;
+  return GFX_OK;
+}
+
+static gfx_status read_loop(gfx_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->loop_host, ctx->loop, sizeof(LoopState), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+static gfx_status write_loop(gfx_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->loop, ctx->loop_host, sizeof(LoopState), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* res) {
+  if (!ctx || !pin) return fail(ctx, GFX_ERR_ARG, "gfx_overrelax: NULL argument");
+  gfx_or_params p = *pin;
+  if (p.maxit < 1 || p.checkinterval < 1)
+    return fail(ctx, GFX_ERR_ARG, "maxit and checkinterval must be positive");
+  if (p.checkinterval_double <= 0) p.checkinterval_double = p.checkinterval;
+  const int ndir = p.gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  int prec = ctx->precision == GFX_PREC_DOUBLE ? 1 : 0;
+  const bool handover = ctx->precision == GFX_PREC_MIXED;
+  gfx_status s = prepare_g(ctx, prec);
+  if (s) return s;
+  const int hist_need = p.maxit / std::min(p.checkinterval, p.checkinterval_double) + 8;
+  s = ensure_hist(ctx, hist_need);
+  if (s) return s;
+
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, ctx->stream));
+
+  LoopState& H = *ctx->loop_host;
+  std::memset(&H, 0, sizeof(H));
+  H.iter = 0;
+  H.ck = prec == 0 ? p.checkinterval : p.checkinterval_double;
+  H.maxit = p.maxit;
+  H.criterion = p.criterion;
+  H.phase = handover ? 0 : 1;
+  H.hist_cap = ctx->hist_cap;
+  H.eps = p.eps;
+  H.switch_eps = p.switch_eps;
+  H.plateau_ratio = p.plateau_ratio > 0 ? p.plateau_ratio : 1e300;
+  s = write_loop(ctx);
+  if (s) return s;
+
+  int sweeps_single = 0, sweeps_double = 0;
+  // iteration 0: sweep, then the first check (overrelax.cu:710-789)
+  enqueue_sweep(ctx, prec, ndir, p.omega);
+  (prec == 0 ? sweeps_single : sweeps_double)++;
+  enqueue_measure(ctx, prec, prec, ndir);
+  enqueue_reduce(ctx, ndir, true, 0, 0, 0);
+  CK(cudaGetLastError());
+  s = read_loop(ctx);
+  if (s) return s;
+
+  for (;;) {
+    if (H.done == 0) {
+      const int it0 = H.iter;
+      if (p.use_graph) {
+        cudaGraphExec_t ex;
+        s = get_graph(ctx, prec, ndir, H.ck, p.omega, &ex);
+        if (s) return s;
+        const unsigned long long before = ctx->launches;
+        CK(cudaGraphLaunch(ex, ctx->stream));
+        s = read_loop(ctx);
+        if (s) return s;
+        // capture counted one body; add one body per executed iteration
+        ctx->launches = before + (unsigned long long)((H.iter - it0) / H.ck) * (2 * H.ck + 3);
+      } else {
+        while (H.done == 0) {
+          enqueue_body(ctx, prec, ndir, H.ck, p.omega, 0, 0);
+          CK(cudaGetLastError());
+          s = read_loop(ctx);
+          if (s) return s;
+        }
+      }
+      (prec == 0 ? sweeps_single : sweeps_double) += H.iter - it0;
+    }
+    if (H.done == 2) {
+      // FP32 phase finished: widen g (reunitarized in FP64) and verify in FP64
+      s = prepare_g(ctx, 1);
+      if (s) return s;
+      prec = 1;
+      H.phase = 1;
+      H.done = 0;
+      H.prev = 0.0;
+      H.ck = p.checkinterval_double;
+      s = write_loop(ctx);
+      if (s) return s;
+      enqueue_measure(ctx, 1, 1, ndir);
+      enqueue_reduce(ctx, ndir, true, 0, 0, 0);
+      CK(cudaGetLastError());
+      s = read_loop(ctx);
+      if (s) return s;
+      continue;
+    }
+    break;
+  }
+  bool converged = H.done == 1;
+  if (!converged) {
+    // tail: the iterations after the last check run without a check (overrelax.cu:710-805)
+    const int tail = p.maxit - 1 - H.iter;
+    for (int k = 0; k < tail; k++) enqueue_sweep(ctx, prec, ndir, p.omega);
+    (prec == 0 ? sweeps_single : sweeps_double) += tail > 0 ? tail : 0;
+    if (prec == 0 && handover) {
+      s = prepare_g(ctx, 1);
+      if (s) return s;
+      prec = 1;
+    }
+  }
+  CK(cudaEventRecord(e1, ctx->stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+
+  const int nrec = std::min(H.nhist, H.hist_cap);
+  ctx->last_hist.resize(nrec);
+  if (nrec > 0 && p.record_history)
+    CK(cudaMemcpy(ctx->last_hist.data(), ctx->hist, sizeof(CheckRecord) * nrec,
+                  cudaMemcpyDeviceToHost));
+  if (!p.record_history) ctx->last_hist.clear();
+  if (res) {
+    std::memset(res, 0, sizeof(*res));
+    res->converged = converged ? 1 : 0;
+    // reference semantics: the converging check's iteration, or -1 (maxit when the
+    // last value equals eps exactly, overrelax.cu:816-822)
+    double last = H.criterion == 0 ? H.last_max : H.criterion == 1 ? H.last_theta
+                                                                    : H.last_theta_slice_max;
+    res->iterations = converged ? H.iter : (last > p.eps ? -1 : p.maxit);
+    res->sweeps_single = sweeps_single;
+    res->sweeps_double = sweeps_double;
+    res->sweeps = sweeps_single + sweeps_double;
+    res->checks = H.nhist;
+    res->final_values.F = H.last_F;
+    res->final_values.dAdA = H.last_dAdA;
+    res->final_values.maxdAdA = H.last_max;
+    res->final_values.theta = H.last_theta;
+    res->final_values.theta_slice_max = H.last_theta_slice_max;
+    res->ms = ms;
+  }
+  return converged ? GFX_OK : GFX_ERR_NOT_CONVERGED;
+}
+
+int gfx_or_history(const gfx_ctx* ctx, gfx_check_record* out, int cap) {
+  if (!ctx) return 0;
+  const int n = std::min((int)ctx->last_hist.size(), cap);
+  for (int k = 0; k < n; k++) {
+    const CheckRecord& r = ctx->last_hist[k];
+    out[k].iter = r.iter;
+    out[k].phase = r.phase;
+    out[k].F = r.F;
+    out[k].dAdA = r.dAdA;
+    out[k].maxdAdA = r.maxdAdA;
+    out[k].theta = r.theta;
+    out[k].theta_slice_max = r.theta_slice_max;
+  }
+  return (int)ctx->last_hist.size();
+}
+
+// ---------------------------------------------------------------------------
+// Mersenne Twister bank
+// ---------------------------------------------------------------------------
+static gfx_status mt_alloc(gfx_ctx* ctx) {
+  if (ctx->bank.a) return GFX_OK;
+  gfx_status s;
+  if ((s = dalloc(ctx, (void**)&ctx->bank.a, 4 * kMTCount))) return s;
+  if ((s = dalloc(ctx, (void**)&ctx->bank.b, 4 * kMTCount))) return s;
+  if ((s = dalloc(ctx, (void**)&ctx->bank.c, 4 * kMTCount))) return s;
+  if ((s = dalloc(ctx, (void**)&ctx->bank.seed, 4 * kMTCount))) return s;
+  if ((s = dalloc(ctx, (void**)&ctx->bank.status, 4 * kMTCount * kMTN))) return s;
+  return GFX_OK;
+}
+
+static gfx_status mt_upload(gfx_ctx* ctx) {
+  std::vector<uint32_t> a(kMTCount), b(kMTCount), c(kMTCount), sd(kMTCount);
+  for (int r = 0; r < kMTCount; r++) {
+    a[r] = ctx->h_params[4 * r];
+    b[r] = ctx->h_params[4 * r + 1];
+    c[r] = ctx->h_params[4 * r + 2];
+    sd[r] = ctx->h_params[4 * r + 3];
+  }
+  CK(cudaMemcpy(ctx->bank.a, a.data(), 4 * kMTCount, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->bank.b, b.data(), 4 * kMTCount, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->bank.c, c.data(), 4 * kMTCount, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->bank.seed, sd.data(), 4 * kMTCount, cudaMemcpyHostToDevice));
+  return GFX_OK;
+}
+
+gfx_status gfx_mt_load_params(gfx_ctx* ctx, const uint32_t* params) {
+  if (!ctx || !params) return fail(ctx, GFX_ERR_ARG, "gfx_mt_load_params: NULL argument");
+  gfx_status s = mt_alloc(ctx);
+  if (s) return s;
+  std::memcpy(ctx->h_params, params, sizeof(ctx->h_params));
+  ctx->mt_params = true;
+  ctx->mt_seeded = false;
+  ctx->mt_init = false;
+  return mt_upload(ctx);
+}
+
+// loadMTGPU (MersenneTwister.cu:79-92): 4096 x {matrix_a, mask_b, mask_c, seed},
+// little-endian uint32
+gfx_status gfx_mt_load_file(gfx_ctx* ctx, const char* path) {
+  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_mt_load_file: NULL argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(ctx, GFX_ERR_IO, std::string("cannot open twister parameters ") + path);
+  std::vector<uint32_t> buf(4 * kMTCount);
+  unsigned char raw[16 * kMTCount];
+  size_t n = std::fread(raw, 1, sizeof(raw), f);
+  std::fclose(f);
+  if (n != sizeof(raw))
+    return fail(ctx, GFX_ERR_IO, std::string("twister parameter file truncated: ") + path);
+  for (int k = 0; k < 4 * kMTCount; k++)
+    buf[k] = (uint32_t)raw[4 * k] | ((uint32_t)raw[4 * k + 1] << 8) |
+             ((uint32_t)raw[4 * k + 2] << 16) | ((uint32_t)raw[4 * k + 3] << 24);
+  return gfx_mt_load_params(ctx, buf.data());
+}
+
+gfx_status gfx_mt_set_seeds(gfx_ctx* ctx, const uint32_t* seeds) {
+  if (!ctx || !seeds) return fail(ctx, GFX_ERR_ARG, "gfx_mt_set_seeds: NULL argument");
+  if (!ctx->mt_params) return fail(ctx, GFX_ERR_STATE, "twister parameters not loaded");
+  for (int r = 0; r < kMTCount; r++) ctx->h_params[4 * r + 3] = seeds[r];
+  ctx->mt_seeded = true;
+  return mt_upload(ctx);
+}
+
+gfx_status gfx_mt_seed(gfx_ctx* ctx, unsigned int mtseed) {
+  std::vector<int32_t> r(kMTCount);
+  gfx_glibc_rand(mtseed, kMTCount, r.data());
+  std::vector<uint32_t> s(kMTCount);
+  for (int k = 0; k < kMTCount; k++) s[k] = (uint32_t)r[k];
+  return gfx_mt_set_seeds(ctx, s.data());
+}
+
+static int align_up2(int q) { return (q % 2) ? q + 1 : q; }
+static int nper_of(int n) { return align_up2(n % kMTCount ? n / kMTCount + 1 : n / kMTCount); }
+
+gfx_status gfx_mt_init(gfx_ctx* ctx, int n_gauss, int n_unif) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (!ctx->mt_params || !ctx->mt_seeded)
+    return fail(ctx, GFX_ERR_STATE, "twister bank needs parameters and seeds before init");
+  if (n_gauss < 1 || n_unif < 1) return fail(ctx, GFX_ERR_ARG, "field sizes must be positive");
+  if (ctx->gauss) {
+    cudaFree(ctx->gauss);
+    ctx->dev_bytes -= sizeof(float) * (size_t)kMTCount * ctx->nper_g;
+    ctx->gauss = nullptr;
+  }
+  if (ctx->unif) {
+    cudaFree(ctx->unif);
+    ctx->dev_bytes -= sizeof(float) * (size_t)kMTCount * ctx->nper_u;
+    ctx->unif = nullptr;
+  }
+  ctx->n_gauss = n_gauss;
+  ctx->n_unif = n_unif;
+  ctx->nper_g = nper_of(n_gauss);
+  ctx->nper_u = nper_of(n_unif);
+  gfx_status s;
+  if ((s = dalloc(ctx, (void**)&ctx->gauss, sizeof(float) * (size_t)kMTCount * ctx->nper_g))) return s;
+  if ((s = dalloc(ctx, (void**)&ctx->unif, sizeof(float) * (size_t)kMTCount * ctx->nper_u))) return s;
+  s = mt_upload(ctx);
+  if (s) return s;
+  launch_mt_generate(ctx->bank, ctx->gauss, ctx->nper_g, 0, 1, ctx->stream);
+  launch_mt_generate(ctx->bank, ctx->unif, ctx->nper_u, 0, 0, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->mt_init = true;
+  return GFX_OK;
+}
+
+static void enqueue_mt_update(gfx_ctx* ctx) {
+  launch_mt_generate(ctx->bank, ctx->gauss, ctx->nper_g, 1, 1, ctx->stream);
+  launch_mt_generate(ctx->bank, ctx->unif, ctx->nper_u, 1, 0, ctx->stream);
+}
+
+gfx_status gfx_mt_update(gfx_ctx* ctx) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "update_MT before init_MT");
+  enqueue_mt_update(ctx);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_mt_sizes(const gfx_ctx* ctx, int* nper_gauss, int* nper_unif) {
+  if (!ctx) return GFX_ERR_ARG;
+  if (nper_gauss) *nper_gauss = ctx->nper_g;
+  if (nper_unif) *nper_unif = ctx->nper_u;
+  return GFX_OK;
+}
+
+gfx_status gfx_mt_read(gfx_ctx* ctx, float* gauss, float* unif, uint32_t* state,
+                       uint32_t* seeds) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "twister bank not initialized");
+  if (gauss)
+    CK(cudaMemcpyAsync(gauss, ctx->gauss, sizeof(float) * (size_t)kMTCount * ctx->nper_g,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (unif)
+    CK(cudaMemcpyAsync(unif, ctx->unif, sizeof(float) * (size_t)kMTCount * ctx->nper_u,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (state)
+    CK(cudaMemcpyAsync(state, ctx->bank.status, 4 * (size_t)kMTCount * kMTN,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (seeds)
+    CK(cudaMemcpyAsync(seeds, ctx->bank.seed, 4 * (size_t)kMTCount, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// simulated annealing (simulated_annealing.cu:265-476)
+// ---------------------------------------------------------------------------
+double gfx_sa_temperature(const gfx_sa_params* p, int i) {
+  double a, temperature;
+  if (p->Tmax == p->Tmin) {
+    temperature = p->Tmax;
+  } else if (p->expo == 0) {
+    a = (double)i / (double)(p->N - 1);
+    temperature = std::pow(p->Tmin / p->Tmax, a) * p->Tmax;
+  } else if (p->expo == -1) {
+    a = (p->Tmin - p->Tmax) / (double)(p->N - 1);
+    temperature = a * i + p->Tmax;
+  } else {
+    a = std::pow(p->Tmin, -p->expo) - std::pow(p->Tmax, -p->expo);
+    a = a / (double)(p->N - 1);
+    temperature = std::pow(a * i + std::pow(p->Tmax, -p->expo), -1.0 / p->expo);
+  }
+  return temperature;
+}
+
+static gfx_status check_sa_fields(gfx_ctx* ctx) {
+  if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "simulated annealing needs init_MT");
+  if ((long long)kMTCount * ctx->nper_g < ctx->vol / 2 ||
+      (long long)kMTCount * ctx->nper_u < 2 * ctx->vol)
+    return fail(ctx, GFX_ERR_STATE, "random fields smaller than V/2 gauss + 2V uniform");
+  return GFX_OK;
+}
+
+gfx_status gfx_sa_halfsweep(gfx_ctx* ctx, int parity, double beta, int precision) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  gfx_status s = check_sa_fields(ctx);
+  if (s) return s;
+  const int prec = precision == 0 ? 0 : 1;
+  if ((s = prepare_g(ctx, prec))) return s;
+  launch_sa_heatbath(prec, ctx->link_nr, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
+                     prec == 0 ? ctx->G32 : ctx->G64, parity, beta, ctx->gauss, ctx->unif,
+                     ctx->block, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_micro_halfsweep(gfx_ctx* ctx, int parity, int gauge, int precision) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  const int prec = precision == 0 ? 0 : 1;
+  gfx_status s = prepare_g(ctx, prec);
+  if (s) return s;
+  launch_micro(prec, ctx->link_nr, gauge == GFX_GAUGE_COULOMB ? 3 : 4, ctx->L,
+               prec == 0 ? ctx->U32 : ctx->U64, prec == 0 ? ctx->G32 : ctx->G64, parity,
+               ctx->block, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_simanneal_range(gfx_ctx* ctx, const gfx_sa_params* p, int first, int count) {
+  if (!ctx || !p) return fail(ctx, GFX_ERR_ARG, "gfx_simanneal_range: NULL argument");
+  if (p->N < 1 || first < 0 || count < 0 || first + count > p->N)
+    return fail(ctx, GFX_ERR_ARG, "SA step range outside [0, N)");
+  gfx_status s = check_sa_fields(ctx);
+  if (s) return s;
+  const int prec = ctx->precision == GFX_PREC_DOUBLE ? 1 : 0;
+  if ((s = prepare_g(ctx, prec))) return s;
+  const void* U = prec == 0 ? ctx->U32 : ctx->U64;
+  void* G = prec == 0 ? ctx->G32 : ctx->G64;
+  for (int i = first; i < first + count; i++) {
+    // set_sa_temperature: beta = 1/T (simulated_annealing.cu:292)
+    const double beta = 1.0 / gfx_sa_temperature(p, i);
+    for (int par = 0; par < 2; par++) {
+      launch_sa_heatbath(prec, ctx->link_nr, ctx->L, U, G, par, beta, ctx->gauss, ctx->unif,
+                         ctx->block, ctx->stream);
+      enqueue_mt_update(ctx);
+    }
+    for (int m = 0; m < p->nmicro; m++)
+      for (int par = 0; par < 2; par++)
+        launch_micro(prec, ctx->link_nr, 4, ctx->L, U, G, par, ctx->block, ctx->stream);
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_simanneal(gfx_ctx* ctx, const gfx_sa_params* p, gfx_functional_t* last) {
+  gfx_status s = gfx_simanneal_range(ctx, p, 0, p ? p->N : 0);
+  if (s) return s;
+  if (last) return gfx_functional(ctx, GFX_GAUGE_LANDAU, 1, last);
+  return GFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// thermalization (heatbath_thermalization.cu:557-841)
+// ---------------------------------------------------------------------------
+gfx_status gfx_link_heatbath_halfsweep(gfx_ctx* ctx, int parity, int nu, double beta) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "link heatbath needs init_MT");
+  if ((long long)kMTCount * ctx->nper_g < 2 * ctx->vol ||
+      (long long)kMTCount * ctx->nper_u < 8 * ctx->vol)
+    return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
+  launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, parity, nu, beta / 3.0, ctx->gauss,
+                       ctx->unif, 128, ctx->stream);
+  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq, int plaq_cap) {
+  if (!ctx || !p) return fail(ctx, GFX_ERR_ARG, "gfx_thermalize: NULL argument");
+  if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "thermalization needs init_MT");
+  if ((long long)kMTCount * ctx->nper_g < 2 * ctx->vol ||
+      (long long)kMTCount * ctx->nper_u < 8 * ctx->vol)
+    return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
+  const double beta3 = p->beta / 3.0;
+  const int checkint = p->checkint > 0 ? p->checkint : p->Nsweep + 1;
+  int np = 0;
+  for (int i = 0; i < p->Nsweep; i++) {
+    for (int nu = 0; nu < 4; nu++)
+      for (int par = 0; par < 2; par++) {
+        launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, par, nu, beta3, ctx->gauss,
+                             ctx->unif, 128, ctx->stream);
+        enqueue_mt_update(ctx);
+      }
+    if (i % checkint == 0 && plaq && np < plaq_cap) {
+      launch_plaquette(ctx->link_nr, ctx->L, ctx->U64, ctx->partials, (double*)ctx->reduced,
+                       ctx->stream);
+      CK(cudaMemcpyAsync(plaq + np, ctx->reduced, sizeof(double), cudaMemcpyDeviceToHost,
+                         ctx->stream));
+      np++;
+    }
+  }
+  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision,
+                           double* ms) {
+  if (!ctx || !ms || nsweeps < 1) return fail(ctx, GFX_ERR_ARG, "gfx_time_sweeps: bad argument");
+  const int prec = precision == 0 ? 0 : 1;
+  gfx_status s = prepare_g(ctx, prec);
+  if (s) return s;
+  const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaEventRecord(e0, ctx->stream));
+  for (int k = 0; k < nsweeps; k++) enqueue_sweep(ctx, prec, ndir, omega);
+  CK(cudaEventRecord(e1, ctx->stream));
+  CK(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = t;
+  return GFX_OK;
+}
+
+unsigned long long gfx_launch_count(const gfx_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+void* gfx_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void gfx_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

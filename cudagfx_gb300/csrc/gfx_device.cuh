@@ -1,0 +1,502 @@
+// gfx_device.cuh -- device-side building blocks for the sm_103a gauge-fixing kernels.
+//
+//  * SU(3) algebra on register-resident 3x3 complex matrices, templated on the
+//    arithmetic type (float for the bulk sweeps, double for the polish sweeps and
+//    the reference-precision path).  The update formulas follow the reference's
+//    device library (dev_su3.cu:1321-1634) and overrelax.cu:149-269.
+//  * Even/odd structure-of-arrays field layout (see Field below).
+//  * Site <-> coordinate arithmetic for the checkerboard index, with neighbours
+//    computed on the fly instead of the reference's gathered nn[] table
+//    (cudagaugefix.cu:72-196).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gfx {
+
+// ---------------------------------------------------------------------------
+// complex / matrix types
+// ---------------------------------------------------------------------------
+template <typename T>
+struct cplx {
+  T re, im;
+};
+
+template <typename T>
+struct Mat3 {
+  cplx<T> e[3][3];
+};
+
+template <typename T>
+__device__ __forceinline__ cplx<T> cmk(T re, T im) {
+  cplx<T> r;
+  r.re = re;
+  r.im = im;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
+  return cmk<T>(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+// a * conj(b)
+template <typename T>
+__device__ __forceinline__ cplx<T> cmulc(cplx<T> a, cplx<T> b) {
+  return cmk<T>(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) {
+  return cmk<T>(a.re + b.re, a.im + b.im);
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> csub(cplx<T> a, cplx<T> b) {
+  return cmk<T>(a.re - b.re, a.im - b.im);
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> cconj(cplx<T> a) {
+  return cmk<T>(a.re, -a.im);
+}
+
+template <typename T>
+__device__ __forceinline__ T rsqrt_t(T x);
+template <>
+__device__ __forceinline__ float rsqrt_t<float>(float x) {
+  return rsqrtf(x);
+}
+template <>
+__device__ __forceinline__ double rsqrt_t<double>(double x) {
+  return rsqrt(x);
+}
+
+template <typename T>
+__device__ __forceinline__ void mzero(Mat3<T>& m) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) m.e[i][j] = cmk<T>(T(0), T(0));
+}
+
+// row 2 = conj(row0 x row1): the 12-real reconstruction (dev_su3.cu:288-305)
+template <typename T>
+__device__ __forceinline__ void row2_from_01(Mat3<T>& g) {
+  g.e[2][0] = cconj(csub(cmul(g.e[0][1], g.e[1][2]), cmul(g.e[0][2], g.e[1][1])));
+  g.e[2][1] = cconj(csub(cmul(g.e[0][2], g.e[1][0]), cmul(g.e[0][0], g.e[1][2])));
+  g.e[2][2] = cconj(csub(cmul(g.e[0][0], g.e[1][1]), cmul(g.e[0][1], g.e[1][0])));
+}
+
+// s += a * b
+template <typename T>
+__device__ __forceinline__ void addmul(Mat3<T>& s, const Mat3<T>& a, const Mat3<T>& b) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      T re = s.e[i][j].re, im = s.e[i][j].im;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re += a.e[i][k].re * b.e[k][j].re - a.e[i][k].im * b.e[k][j].im;
+        im += a.e[i][k].re * b.e[k][j].im + a.e[i][k].im * b.e[k][j].re;
+      }
+      s.e[i][j] = cmk<T>(re, im);
+    }
+}
+
+// s += a * b^+
+template <typename T>
+__device__ __forceinline__ void addmul_nd(Mat3<T>& s, const Mat3<T>& a, const Mat3<T>& b) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      T re = s.e[i][j].re, im = s.e[i][j].im;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re += a.e[i][k].re * b.e[j][k].re + a.e[i][k].im * b.e[j][k].im;
+        im += a.e[i][k].im * b.e[j][k].re - a.e[i][k].re * b.e[j][k].im;
+      }
+      s.e[i][j] = cmk<T>(re, im);
+    }
+}
+
+// s += (b * a)^+  = a^+ b^+ ; used for the backward star term U^+(x-mu) g^+(x-mu)
+template <typename T>
+__device__ __forceinline__ void addmul_dd(Mat3<T>& s, const Mat3<T>& a, const Mat3<T>& b) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      // (a^+ b^+)_ij = sum_k conj(a_ki) conj(b_jk) = conj(sum_k b_jk a_ki)
+      T re = T(0), im = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        re += b.e[j][k].re * a.e[k][i].re - b.e[j][k].im * a.e[k][i].im;
+        im += b.e[j][k].re * a.e[k][i].im + b.e[j][k].im * a.e[k][i].re;
+      }
+      s.e[i][j].re += re;
+      s.e[i][j].im -= im;
+    }
+}
+
+// r = a * b
+template <typename T>
+__device__ __forceinline__ void mul(Mat3<T>& r, const Mat3<T>& a, const Mat3<T>& b) {
+  mzero(r);
+  addmul(r, a, b);
+}
+
+// (a*b)_ij for one entry
+template <typename T>
+__device__ __forceinline__ cplx<T> mul_entry(const Mat3<T>& a, const Mat3<T>& b, int i, int j) {
+  T re = T(0), im = T(0);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    re += a.e[i][k].re * b.e[k][j].re - a.e[i][k].im * b.e[k][j].im;
+    im += a.e[i][k].re * b.e[k][j].im + a.e[i][k].im * b.e[k][j].re;
+  }
+  return cmk<T>(re, im);
+}
+
+// Gram-Schmidt on rows 0,1 (dev_su3.cu:1569-1615); row 2 only when asked
+template <typename T, bool ROW2>
+__device__ __forceinline__ void normalize(Mat3<T>& u) {
+  T len = u.e[0][0].re * u.e[0][0].re + u.e[0][0].im * u.e[0][0].im + u.e[0][1].re * u.e[0][1].re +
+          u.e[0][1].im * u.e[0][1].im + u.e[0][2].re * u.e[0][2].re + u.e[0][2].im * u.e[0][2].im;
+  len = rsqrt_t<T>(len);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    u.e[0][i].re *= len;
+    u.e[0][i].im *= len;
+  }
+  cplx<T> proj = cmk<T>(T(0), T(0));
+#pragma unroll
+  for (int i = 0; i < 3; i++) proj = cadd(proj, cmulc(u.e[1][i], u.e[0][i]));
+#pragma unroll
+  for (int i = 0; i < 3; i++) u.e[1][i] = csub(u.e[1][i], cmul(proj, u.e[0][i]));
+  len = u.e[1][0].re * u.e[1][0].re + u.e[1][0].im * u.e[1][0].im + u.e[1][1].re * u.e[1][1].re +
+        u.e[1][1].im * u.e[1][1].im + u.e[1][2].re * u.e[1][2].re + u.e[1][2].im * u.e[1][2].im;
+  len = rsqrt_t<T>(len);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    u.e[1][i].re *= len;
+    u.e[1][i].im *= len;
+  }
+  if (ROW2) row2_from_01(u);
+}
+
+// ---------------------------------------------------------------------------
+// SU(2) subgroup updates.  A subgroup element is the 4-vector
+// (w0, w1, w2, w3) = (a.x, a.y, b.x, b.y) of the reference (overrelax.cu:184-198).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct Su2 {
+  T v[4];
+};
+
+// w of subgroup (a,b) of X = g * star (overrelax.cu:217-223); only four entries of X
+template <typename T>
+__device__ __forceinline__ Su2<T> su2_extract(const Mat3<T>& g, const Mat3<T>& star, int a, int b) {
+  cplx<T> xaa = mul_entry(g, star, a, a);
+  cplx<T> xbb = mul_entry(g, star, b, b);
+  cplx<T> xab = mul_entry(g, star, a, b);
+  cplx<T> xba = mul_entry(g, star, b, a);
+  Su2<T> w;
+  w.v[0] = xaa.re + xbb.re;
+  w.v[3] = -xaa.im + xbb.im;
+  w.v[1] = -xab.im - xba.im;
+  w.v[2] = -xab.re + xba.re;
+  return w;
+}
+
+// rows a,b of g <- alpha acting from the left (overrelax.cu:244-265)
+template <typename T>
+__device__ __forceinline__ void su2_rotate(Mat3<T>& g, int a, int b, const Su2<T>& al) {
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    cplx<T> ga = g.e[a][c], gb = g.e[b][c];
+    cplx<T> na = cadd(cmul(cmk<T>(al.v[0], al.v[3]), ga), cmul(cmk<T>(al.v[2], al.v[1]), gb));
+    cplx<T> nb = cadd(cmul(cmk<T>(-al.v[2], al.v[1]), ga), cmul(cmk<T>(al.v[0], -al.v[3]), gb));
+    g.e[a][c] = na;
+    g.e[b][c] = nb;
+  }
+}
+
+// SU(2) subgroups in the reference's order: (0,1), (0,2), (1,2)
+__device__ __forceinline__ int sub_a(int s) { return s == 2 ? 1 : 0; }
+__device__ __forceinline__ int sub_b(int s) { return s == 0 ? 1 : 2; }
+
+// Cabibbo-Marinari relaxation (overrelax.cu:203-269)
+template <typename T>
+__device__ __forceinline__ void cm_relax(Mat3<T>& g, const Mat3<T>& star) {
+#pragma unroll
+  for (int s = 0; s < 3; s++) {
+    const int a = sub_a(s), b = sub_b(s);
+    Su2<T> w = su2_extract(g, star, a, b);
+    T det = rsqrt_t<T>(w.v[0] * w.v[0] + w.v[1] * w.v[1] + w.v[2] * w.v[2] + w.v[3] * w.v[3]);
+#pragma unroll
+    for (int k = 0; k < 4; k++) w.v[k] *= det;
+    su2_rotate(g, a, b, w);
+  }
+}
+
+// Micro-overrelaxation: alpha = (2 w0/|w|^2) w - 1, i.e. the square of the relaxed
+// subgroup element (heatbath_thermalization.cu:318-401)
+template <typename T>
+__device__ __forceinline__ void cm_micro(Mat3<T>& g, const Mat3<T>& star) {
+#pragma unroll
+  for (int s = 0; s < 3; s++) {
+    const int a = sub_a(s), b = sub_b(s);
+    Su2<T> w = su2_extract(g, star, a, b);
+    T tr = w.v[0] * w.v[0] + w.v[1] * w.v[1] + w.v[2] * w.v[2] + w.v[3] * w.v[3];
+    Su2<T> al;
+    if (fabs((double)tr) < 1.0e-9) {
+      al.v[0] = T(1);
+      al.v[1] = al.v[2] = al.v[3] = T(0);
+    } else {
+      T fac = T(2) * w.v[0] / tr;
+#pragma unroll
+      for (int k = 0; k < 4; k++) al.v[k] = fac * w.v[k];
+      al.v[0] -= T(1);
+    }
+    su2_rotate(g, a, b, al);
+  }
+}
+
+// Overrelaxation step of overrelax.cu:149-177, 411-417:
+//   g_new = normalize( normalize(Rw) g_old ),  Rw = 1 + w R + w(w-1)/2 R^2,
+//   R = g_relax g_old^+ - 1.
+// For g_old in SU(3), normalize(Rw) g_old = normalize(Rw g_old), and
+//   Rw g_old = g_old + w D + w(w-1)/2 (D g_old^+) D,  D = g_relax - g_old,
+// so only rows 0,1 of the result are formed (they are all that is stored).
+template <typename T>
+__device__ __forceinline__ void overrelax_rows01(Mat3<T>& gout, const Mat3<T>& gold,
+                                                 const Mat3<T>& grelax, T omega) {
+  Mat3<T> D;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) D.e[i][j] = csub(grelax.e[i][j], gold.e[i][j]);
+  const T c2 = omega * (omega - T(1)) * T(0.5);
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    // R_rk = (D gold^+)_rk
+    cplx<T> R[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      T re = T(0), im = T(0);
+#pragma unroll
+      for (int l = 0; l < 3; l++) {
+        re += D.e[r][l].re * gold.e[k][l].re + D.e[r][l].im * gold.e[k][l].im;
+        im += D.e[r][l].im * gold.e[k][l].re - D.e[r][l].re * gold.e[k][l].im;
+      }
+      R[k] = cmk<T>(re, im);
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      T re = gold.e[r][j].re + omega * D.e[r][j].re;
+      T im = gold.e[r][j].im + omega * D.e[r][j].im;
+      T rr = T(0), ri = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        rr += R[k].re * D.e[k][j].re - R[k].im * D.e[k][j].im;
+        ri += R[k].re * D.e[k][j].im + R[k].im * D.e[k][j].re;
+      }
+      gout.e[r][j] = cmk<T>(re + c2 * rr, im + c2 * ri);
+    }
+  }
+  normalize<T, false>(gout);
+}
+
+// ---------------------------------------------------------------------------
+// Field layout in HBM
+// ---------------------------------------------------------------------------
+// A field of n matrices per (parity, slot) is stored as NCHUNK planes of 16-byte
+// vectors: plane c holds chunk c of every matrix, so consecutive threads
+// (consecutive checkerboard sites) read consecutive 16-byte words -- one
+// fully coalesced 128-bit load per chunk.
+//   FP32, 12 reals: 3 chunks of float4  (row0 = c0.xyzw, c1.xy; row1 = c1.zw, c2.xyzw)
+//   FP64, 12 reals: 6 chunks of double2 (one complex number per chunk)
+//   FP64, 18 reals: 9 chunks of double2 (rows 0..2, no reconstruction)
+template <typename T>
+struct VecOf;
+template <>
+struct VecOf<float> {
+  typedef float4 type;
+};
+template <>
+struct VecOf<double> {
+  typedef double2 type;
+};
+
+template <typename T, int NR>
+struct Field {
+  typedef typename VecOf<T>::type V;
+  static constexpr int NCHUNK = NR * (int)sizeof(T) / 16;
+
+  // load matrix i of the block starting at base (planes spaced by stride vectors)
+  __device__ static __forceinline__ void load(const V* __restrict__ base, size_t stride, int i,
+                                              Mat3<T>& m);
+  __device__ static __forceinline__ void store(V* __restrict__ base, size_t stride, int i,
+                                               const Mat3<T>& m);
+};
+
+template <typename T>
+__device__ __forceinline__ T* mat_scalar(Mat3<T>& m, int k) {
+  // k in [0,18): row-major complex entries, re/im interleaved
+  return (&m.e[0][0].re) + k;
+}
+
+__device__ __forceinline__ float4 ldg_stream(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ double2 ldg_stream(const double2* p) { return __ldg(p); }
+
+template <>
+__device__ __forceinline__ void Field<float, 12>::load(const float4* __restrict__ base,
+                                                       size_t stride, int i, Mat3<float>& m) {
+  float4 a = __ldg(base + i);
+  float4 b = __ldg(base + stride + i);
+  float4 c = __ldg(base + 2 * stride + i);
+  m.e[0][0] = cmk(a.x, a.y);
+  m.e[0][1] = cmk(a.z, a.w);
+  m.e[0][2] = cmk(b.x, b.y);
+  m.e[1][0] = cmk(b.z, b.w);
+  m.e[1][1] = cmk(c.x, c.y);
+  m.e[1][2] = cmk(c.z, c.w);
+  row2_from_01(m);
+}
+template <>
+__device__ __forceinline__ void Field<float, 12>::store(float4* __restrict__ base, size_t stride,
+                                                        int i, const Mat3<float>& m) {
+  base[i] = make_float4(m.e[0][0].re, m.e[0][0].im, m.e[0][1].re, m.e[0][1].im);
+  base[stride + i] = make_float4(m.e[0][2].re, m.e[0][2].im, m.e[1][0].re, m.e[1][0].im);
+  base[2 * stride + i] = make_float4(m.e[1][1].re, m.e[1][1].im, m.e[1][2].re, m.e[1][2].im);
+}
+template <>
+__device__ __forceinline__ void Field<double, 12>::load(const double2* __restrict__ base,
+                                                        size_t stride, int i, Mat3<double>& m) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    double2 v = __ldg(base + k * stride + i);
+    m.e[k / 3][k % 3] = cmk(v.x, v.y);
+  }
+  row2_from_01(m);
+}
+template <>
+__device__ __forceinline__ void Field<double, 12>::store(double2* __restrict__ base,
+                                                         size_t stride, int i,
+                                                         const Mat3<double>& m) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) base[k * stride + i] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+}
+template <>
+__device__ __forceinline__ void Field<double, 18>::load(const double2* __restrict__ base,
+                                                        size_t stride, int i, Mat3<double>& m) {
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    double2 v = __ldg(base + k * stride + i);
+    m.e[k / 3][k % 3] = cmk(v.x, v.y);
+  }
+}
+template <>
+__device__ __forceinline__ void Field<double, 18>::store(double2* __restrict__ base,
+                                                         size_t stride, int i,
+                                                         const Mat3<double>& m) {
+#pragma unroll
+  for (int k = 0; k < 9; k++) base[k * stride + i] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+}
+
+// ---------------------------------------------------------------------------
+// Lattice geometry
+// ---------------------------------------------------------------------------
+// Division by a runtime constant d <= 2^31 for dividends n < 2^31:
+// q = (n * m) >> s with m = ceil(2^s / d), s = 31 + ceil(log2 d)  (round-up method).
+struct FastDiv {
+  uint32_t d, m, s;
+};
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  return (uint32_t)(((unsigned long long)n * f.m) >> f.s);
+}
+
+// Checkerboard index of parity p: i = xh + LXh*(y + LY*(z + LZ*t)), x = 2*xh + ((p+y+z+t)&1).
+// It equals the reference's lexic2eo numbering (cudagaugefix.cu:129-196) for even LX.
+struct Lattice {
+  int lx, ly, lz, lt;  // extents (all even)
+  int lxh;             // lx/2
+  int vh;              // V/2
+  int sy, sz, st;      // eo-index strides of y, z, t
+  FastDiv d_lxh, d_ly, d_lz;
+};
+
+struct Site {
+  int i, xh, y, z, t, s;  // s = x & 1
+};
+
+__device__ __forceinline__ Site site_of(const Lattice& L, int i, int parity) {
+  Site c;
+  c.i = i;
+  uint32_t r = fdiv((uint32_t)i, L.d_lxh);
+  c.xh = i - (int)r * L.lxh;
+  uint32_t r2 = fdiv(r, L.d_ly);
+  c.y = (int)r - (int)r2 * L.ly;
+  uint32_t r3 = fdiv(r2, L.d_lz);
+  c.z = (int)r2 - (int)r3 * L.lz;
+  c.t = (int)r3;
+  c.s = (parity + c.y + c.z + c.t) & 1;
+  return c;
+}
+
+// eo index of the neighbour x + mu (fwd) or x - mu (bwd); it has the opposite parity
+__device__ __forceinline__ int nb_fwd(const Lattice& L, const Site& c, int mu) {
+  switch (mu) {
+    case 0: {
+      int xh = c.xh + c.s;
+      if (xh == L.lxh) xh = 0;
+      return c.i - c.xh + xh;
+    }
+    case 1:
+      return c.y == L.ly - 1 ? c.i - (L.ly - 1) * L.sy : c.i + L.sy;
+    case 2:
+      return c.z == L.lz - 1 ? c.i - (L.lz - 1) * L.sz : c.i + L.sz;
+    default:
+      return c.t == L.lt - 1 ? c.i - (L.lt - 1) * L.st : c.i + L.st;
+  }
+}
+__device__ __forceinline__ int nb_bwd(const Lattice& L, const Site& c, int mu) {
+  switch (mu) {
+    case 0: {
+      int xh = c.xh - (1 - c.s);
+      if (xh < 0) xh = L.lxh - 1;
+      return c.i - c.xh + xh;
+    }
+    case 1:
+      return c.y == 0 ? c.i + (L.ly - 1) * L.sy : c.i - L.sy;
+    case 2:
+      return c.z == 0 ? c.i + (L.lz - 1) * L.sz : c.i - L.sz;
+    default:
+      return c.t == 0 ? c.i + (L.lt - 1) * L.st : c.i - L.st;
+  }
+}
+
+// Pointers to one lattice's fields.  Links: block (p, mu) at U + (p*4+mu)*NCHUNK*vh,
+// plane c of it at +c*vh.  Gauge transformation: block p at G + p*NCHUNK*vh.
+template <typename T, int NRU, int NRG>
+struct FieldPtrs {
+  typedef typename VecOf<T>::type V;
+  const V* U;
+  V* G;
+};
+
+// ---------------------------------------------------------------------------
+// block reductions (FP64 accumulation)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+}  // namespace gfx

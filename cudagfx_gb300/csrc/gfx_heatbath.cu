@@ -1,0 +1,249 @@
+// gfx_heatbath.cu -- stochastic updates for sm_103a:
+//   * simulated-annealing heatbath of the gauge transformation g
+//     (simulated_annealing.cu:5-257),
+//   * microcanonical (SU(2)-reflection) sweep of g,
+//   * Cabibbo-Marinari heatbath of the links for thermalization
+//     (heatbath_thermalization.cu:235-550), storing the result at link (x, nu).
+// Random numbers are read from the Mersenne-Twister fields with the reference's
+// indexing: gauss[k], unif[4k..4k+3] with k = eo index (SA) or 4*eo + nu (links).
+#include "gfx_internal.h"
+
+namespace gfx {
+
+// dev_get_a0 (simulated_annealing.cu:5-27): one single-precision trial
+__device__ __forceinline__ int get_a0(double& a0, double kb, float gauss, float4 u) {
+  float a = fabsf(gauss);
+  float b = -logf(1.0f - u.x);
+  float y = a * a + b;
+  y = (float)((double)y / kb);
+  const float help = u.y;
+  if ((2.0f * (help * help)) <= (2.0f - y)) {
+    a0 = (double)(1.0f - y);
+    return 1;
+  }
+  a0 = 0.0;
+  return 0;
+}
+
+// dev_heatbath_su2 (simulated_annealing.cu:33-73).  k = |w|^2 as in the reference;
+// on rejection alpha = w (unnormalized), which the final reunitarization absorbs.
+template <typename T>
+__device__ __forceinline__ Su2<T> heatbath_su2(const Su2<T>& wt, double beta, float gauss,
+                                               float4 u) {
+  double w[4] = {(double)wt.v[0], (double)wt.v[1], (double)wt.v[2], (double)wt.v[3]};
+  const double k = w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + w[3] * w[3];
+  const double rdet = rsqrt(k);
+  double v[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) v[i] = w[i] * rdet;
+  double a[4];
+  const int ret = get_a0(a[0], k * beta, gauss, u);
+  Su2<T> al;
+  if (ret == 1) {
+    const double norm = sqrt(1.0 - a[0] * a[0]);
+    const double cos_theta = 2.0 * (double)u.z - 1.0;
+    const double sin_theta = sqrt(1.0 - cos_theta * cos_theta);
+    const double phi = 6.2831853071795862 * (double)u.w;
+    double sphi, cphi;
+    sincos(phi, &sphi, &cphi);
+    a[1] = norm * sin_theta * cphi;
+    a[2] = norm * sin_theta * sphi;
+    a[3] = norm * cos_theta;
+    // dev_su2_ti_su2(alpha, a, v) (dev_su3.cu:1385-1399)
+    al.v[0] = (T)(a[0] * v[0] - a[1] * v[1] - a[2] * v[2] - a[3] * v[3]);
+    al.v[1] = (T)(a[0] * v[1] + a[1] * v[0] - a[2] * v[3] + a[3] * v[2]);
+    al.v[2] = (T)(a[0] * v[2] + a[2] * v[0] - a[3] * v[1] + a[1] * v[3]);
+    al.v[3] = (T)(a[0] * v[3] + a[3] * v[0] - a[1] * v[2] + a[2] * v[1]);
+  } else {
+    al = wt;
+  }
+  return al;
+}
+
+// cabibbo_marinari_heatbath (simulated_annealing.cu:81-142): the three subgroups use
+// the same random numbers
+template <typename T>
+__device__ __forceinline__ void cm_heatbath(Mat3<T>& g, const Mat3<T>& star, double beta,
+                                            float gauss, float4 u) {
+#pragma unroll
+  for (int s = 0; s < 3; s++) {
+    const int a = sub_a(s), b = sub_b(s);
+    Su2<T> w = su2_extract(g, star, a, b);
+    Su2<T> al = heatbath_su2(w, beta, gauss, u);
+    su2_rotate(g, a, b, al);
+  }
+}
+
+// star for the gauge-transformation update (same as the OR kernel)
+template <typename T, int NRU, int NDIR>
+__device__ __forceinline__ void g_star(const Lattice& L, const Site& c, int parity,
+                                       const typename VecOf<T>::type* __restrict__ U,
+                                       const typename VecOf<T>::type* __restrict__ G,
+                                       Mat3<T>& star) {
+  constexpr int NCU = Field<T, NRU>::NCHUNK;
+  constexpr int NCG = Field<T, 12>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  const int q = 1 - parity;
+  const typename VecOf<T>::type* Gq = G + (size_t)q * NCG * vh;
+  mzero(star);
+#pragma unroll
+  for (int mu = 0; mu < NDIR; mu++) {
+    Mat3<T> a, b;
+    Field<T, NRU>::load(U + (size_t)(parity * 4 + mu) * NCU * vh, vh, c.i, a);
+    Field<T, 12>::load(Gq, vh, nb_fwd(L, c, mu), b);
+    addmul_nd(star, a, b);
+    const int jb = nb_bwd(L, c, mu);
+    Field<T, NRU>::load(U + (size_t)(q * 4 + mu) * NCU * vh, vh, jb, a);
+    Field<T, 12>::load(Gq, vh, jb, b);
+    addmul_dd(star, a, b);
+  }
+}
+
+template <typename T, int NRU>
+__global__ void __launch_bounds__(256) sa_heatbath_kernel(Lattice L,
+                                                           const typename VecOf<T>::type* U,
+                                                           typename VecOf<T>::type* G, int parity,
+                                                           double beta, const float* gauss,
+                                                           const float4* unif4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  const size_t vh = (size_t)L.vh;
+  const Site c = site_of(L, i, parity);
+  Mat3<T> star, g;
+  g_star<T, NRU, 4>(L, c, parity, U, G, star);
+  typename VecOf<T>::type* Gp = G + (size_t)parity * Field<T, 12>::NCHUNK * vh;
+  Field<T, 12>::load(Gp, vh, i, g);
+  cm_heatbath(g, star, beta, __ldg(gauss + i), __ldg(unif4 + i));
+  normalize<T, false>(g);
+  Field<T, 12>::store(Gp, vh, i, g);
+}
+
+template <typename T, int NRU, int NDIR>
+__global__ void __launch_bounds__(256) micro_kernel(Lattice L, const typename VecOf<T>::type* U,
+                                                     typename VecOf<T>::type* G, int parity) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  const size_t vh = (size_t)L.vh;
+  const Site c = site_of(L, i, parity);
+  Mat3<T> star, g;
+  g_star<T, NRU, NDIR>(L, c, parity, U, G, star);
+  typename VecOf<T>::type* Gp = G + (size_t)parity * Field<T, 12>::NCHUNK * vh;
+  Field<T, 12>::load(Gp, vh, i, g);
+  cm_micro(g, star);
+  normalize<T, false>(g);
+  Field<T, 12>::store(Gp, vh, i, g);
+}
+
+void launch_sa_heatbath(int prec, int link_nr, const Lattice& L, const void* U, void* G,
+                        int parity, double beta, const float* gauss, const float* unif, int block,
+                        cudaStream_t s) {
+  dim3 grid((L.vh + block - 1) / block);
+  const float4* u4 = (const float4*)unif;
+  if (prec == 0)
+    sa_heatbath_kernel<float, 12><<<grid, block, 0, s>>>(L, (const float4*)U, (float4*)G, parity,
+                                                          beta, gauss, u4);
+  else if (link_nr == 18)
+    sa_heatbath_kernel<double, 18><<<grid, block, 0, s>>>(L, (const double2*)U, (double2*)G,
+                                                           parity, beta, gauss, u4);
+  else
+    sa_heatbath_kernel<double, 12><<<grid, block, 0, s>>>(L, (const double2*)U, (double2*)G,
+                                                           parity, beta, gauss, u4);
+}
+
+void launch_micro(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
+                  int parity, int block, cudaStream_t s) {
+  dim3 grid((L.vh + block - 1) / block);
+#define MICRO(T, NR, ND)                                                        \
+  micro_kernel<T, NR, ND><<<grid, block, 0, s>>>(L, (const typename VecOf<T>::type*)U, \
+                                                   (typename VecOf<T>::type*)G, parity)
+  if (prec == 0) {
+    if (ndir == 4) MICRO(float, 12, 4);
+    else MICRO(float, 12, 3);
+  } else if (link_nr == 18) {
+    if (ndir == 4) MICRO(double, 18, 4);
+    else MICRO(double, 18, 3);
+  } else {
+    if (ndir == 4) MICRO(double, 12, 4);
+    else MICRO(double, 12, 3);
+  }
+#undef MICRO
+}
+
+// ---------------------------------------------------------------------------
+// link heatbath (heatbath_thermalization.cu:235-308, 493-550)
+// ---------------------------------------------------------------------------
+struct Coord {
+  int x, y, z, t;
+};
+__device__ __forceinline__ Coord cshift(const Lattice& L, Coord c, int mu, int d) {
+  if (mu == 0) c.x = (c.x + d + L.lx) % L.lx;
+  else if (mu == 1) c.y = (c.y + d + L.ly) % L.ly;
+  else if (mu == 2) c.z = (c.z + d + L.lz) % L.lz;
+  else c.t = (c.t + d + L.lt) % L.lt;
+  return c;
+}
+
+template <int NR>
+__device__ __forceinline__ void ld_link(const Lattice& L, const double2* __restrict__ U, Coord c,
+                                        int mu, Mat3<double>& m) {
+  constexpr int NC = Field<double, NR>::NCHUNK;
+  const int p = (c.x + c.y + c.z + c.t) & 1;
+  const int i = (c.x >> 1) + L.lxh * (c.y + L.ly * (c.z + L.lz * c.t));
+  Field<double, NR>::load(U + (size_t)(p * 4 + mu) * NC * L.vh, (size_t)L.vh, i, m);
+}
+
+template <int NR>
+__global__ void __launch_bounds__(128) link_heatbath_kernel(Lattice L, double2* U, int parity,
+                                                             int nu, double beta3,
+                                                             const float* gauss,
+                                                             const float4* unif4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  const Site s = site_of(L, i, parity);
+  const Coord x = {2 * s.xh + s.s, s.y, s.z, s.t};
+  Mat3<double> staple, h1, h2, h3;
+  mzero(staple);
+#pragma unroll 1
+  for (int mu = 0; mu < 4; mu++) {
+    if (mu == nu) continue;
+    const Coord xpn = cshift(L, x, nu, 1);
+    const Coord xpm = cshift(L, x, mu, 1);
+    const Coord xmm = cshift(L, x, mu, -1);
+    const Coord xpnmm = cshift(L, xpn, mu, -1);
+    // U_mu(x+nu) U_nu^+(x+mu) U_mu^+(x)
+    ld_link<NR>(L, U, xpn, mu, h1);
+    ld_link<NR>(L, U, xpm, nu, h2);
+    mzero(h3);
+    addmul_nd(h3, h1, h2);
+    ld_link<NR>(L, U, x, mu, h1);
+    addmul_nd(staple, h3, h1);
+    // U_mu^+(x+nu-mu) U_nu^+(x-mu) U_mu(x-mu)
+    ld_link<NR>(L, U, xpnmm, mu, h1);
+    ld_link<NR>(L, U, xmm, nu, h2);
+    mzero(h3);
+    addmul_dd(h3, h1, h2);  // h1^+ h2^+
+    ld_link<NR>(L, U, xmm, mu, h1);
+    addmul(staple, h3, h1);
+  }
+  constexpr int NC = Field<double, NR>::NCHUNK;
+  double2* blk = U + (size_t)(parity * 4 + nu) * NC * L.vh;
+  Mat3<double> link;
+  Field<double, NR>::load(blk, (size_t)L.vh, i, link);
+  const int r = 4 * i + nu;
+  cm_heatbath(link, staple, beta3, __ldg(gauss + r), __ldg(unif4 + r));
+  normalize<double, true>(link);
+  Field<double, NR>::store(blk, (size_t)L.vh, i, link);
+}
+
+void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu, double beta3,
+                          const float* gauss, const float* unif, int block, cudaStream_t s) {
+  dim3 grid((L.vh + block - 1) / block);
+  if (link_nr == 18)
+    link_heatbath_kernel<18><<<grid, block, 0, s>>>(L, (double2*)U, parity, nu, beta3, gauss,
+                                                     (const float4*)unif);
+  else
+    link_heatbath_kernel<12><<<grid, block, 0, s>>>(L, (double2*)U, parity, nu, beta3, gauss,
+                                                     (const float4*)unif);
+}
+
+}  // namespace gfx

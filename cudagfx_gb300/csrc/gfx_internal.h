@@ -1,0 +1,93 @@
+// gfx_internal.h -- host-side declarations shared by the library's translation units.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gfx_device.cuh"
+
+namespace gfx {
+
+// Host construction of the lattice descriptor.
+Lattice make_lattice(int lx, int ly, int lz, int lt);
+
+// Per-check record kept on the device (one per functional evaluation).
+struct CheckRecord {
+  int iter;
+  int phase;  // 0 = single-precision sweeps, 1 = double-precision sweeps
+  double F, dAdA, maxdAdA, theta, theta_slice_max;
+};
+
+// Device-resident state of a convergence loop.
+struct LoopState {
+  int iter;       // iteration index of the last check
+  int ck;         // sweeps between checks
+  int maxit;      // iteration cap (exclusive, as in the reference loop)
+  int done;       // 0 running, 1 converged, 2 switch precision, 3 stopped at cap
+  int criterion;  // GFX_CRIT_*
+  int phase;
+  int nhist, hist_cap;
+  double eps;
+  double switch_eps;     // phase 0 -> 1 when the monitored value drops below
+  double plateau_ratio;  // phase 0 -> 1 when value_new > ratio * value_old
+  double prev;
+  double last_F, last_dAdA, last_max, last_theta, last_theta_slice_max;
+};
+
+// Reduction results written by the final reduce kernel.
+struct Reduced {
+  double F, dAdA, maxdAdA, theta, theta_slice_max;
+};
+
+// ----- kernel launchers (gfx_kernels.cu) -----
+// precision tags: 0 = FP32 12-real, 1 = FP64 12-real, 2 = FP64 18-real (links only)
+void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
+                         int parity, double omega, int block, cudaStream_t s);
+// measure: compute precision (0 float, 1 double), g storage (0 float, 1 double)
+void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
+                    const void* G, double* partials, int block, cudaStream_t s);
+int measure_blocks_x(const Lattice& L, int block);
+void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
+                   Reduced* out, LoopState* loop, CheckRecord* hist, int advance,
+                   unsigned long long graph_handle, int use_handle, cudaStream_t s);
+void launch_plaquette(int link_nr_prec, const Lattice& L, const void* U, double* partials,
+                      double* out, cudaStream_t s);
+void launch_polyakov(int link_nr_prec, const Lattice& L, const void* U, double* partials,
+                     double* out, cudaStream_t s);
+void launch_pack_links(int link_nr_prec, const Lattice& L, const double* aos, void* U,
+                       cudaStream_t s);
+void launch_unpack_links(int link_nr_prec, const Lattice& L, const void* U, double* aos,
+                         cudaStream_t s);
+void launch_pack_g(int gprec, const Lattice& L, const double* aos, void* G, cudaStream_t s);
+void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cudaStream_t s);
+void launch_convert_links_64_to_32(int link_nr, const Lattice& L, const void* U64, void* U32,
+                                   cudaStream_t s);
+void launch_convert_g(int from_prec, int to_prec, const Lattice& L, const void* Gin, void* Gout,
+                      cudaStream_t s);
+void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s);
+
+// ----- heatbath family (gfx_heatbath.cu) -----
+void launch_sa_heatbath(int prec, int link_nr, const Lattice& L, const void* U, void* G,
+                        int parity, double beta, const float* gauss, const float* unif,
+                        int block, cudaStream_t s);
+void launch_micro(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
+                  int parity, int block, cudaStream_t s);
+void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu,
+                          double beta3, const float* gauss, const float* unif, int block,
+                          cudaStream_t s);
+
+// ----- Mersenne Twister bank (gfx_mt.cu) -----
+struct MTBank {
+  uint32_t* a;       // matrix_a[4096]
+  uint32_t* b;       // mask_b[4096]
+  uint32_t* c;       // mask_c[4096]
+  uint32_t* seed;    // seed[4096]
+  uint32_t* status;  // [19][4096]
+};
+constexpr int kMTCount = 4096;
+constexpr int kMTN = 19;
+void launch_mt_generate(const MTBank& bank, float* out, int nper, int initialized, int gauss,
+                        cudaStream_t s);
+
+}  // namespace gfx

@@ -1,0 +1,699 @@
+// gfx_kernels.cu -- overrelaxation sweep, functional/theta measurement, reductions,
+// plaquette, Polyakov loop and field-layout kernels for sm_103a.
+#include <cstdio>
+
+#include "gfx_internal.h"
+
+namespace gfx {
+
+Lattice make_lattice(int lx, int ly, int lz, int lt) {
+  Lattice L;
+  L.lx = lx;
+  L.ly = ly;
+  L.lz = lz;
+  L.lt = lt;
+  L.lxh = lx / 2;
+  L.vh = (int)((long long)lx * ly * lz * lt / 2);
+  L.sy = L.lxh;
+  L.sz = L.lxh * ly;
+  L.st = L.lxh * ly * lz;
+  auto mk = [](uint32_t d) {
+    FastDiv f;
+    f.d = d;
+    uint32_t l = 0;
+    while ((1ull << l) < d) l++;
+    f.s = 31 + l;
+    unsigned long long m = ((1ull << f.s) + d - 1) / d;
+    f.m = (uint32_t)m;
+    return f;
+  };
+  L.d_lxh = mk((uint32_t)L.lxh);
+  L.d_ly = mk((uint32_t)ly);
+  L.d_lz = mk((uint32_t)lz);
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// generic loads with precision conversion
+// ---------------------------------------------------------------------------
+template <typename TC, typename TS, int NR>
+struct Load {
+  typedef typename VecOf<TS>::type V;
+  __device__ static __forceinline__ void go(const V* base, size_t stride, int i, Mat3<TC>& m) {
+    Field<TC, NR>::load(base, stride, i, m);
+  }
+};
+// FP64 compute on FP32-stored g: widen rows 0,1 and reunitarize in FP64
+template <>
+struct Load<double, float, 12> {
+  __device__ static __forceinline__ void go(const float4* base, size_t stride, int i,
+                                            Mat3<double>& m) {
+    Mat3<float> f;
+    Field<float, 12>::load(base, stride, i, f);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) m.e[r][c] = cmk<double>(f.e[r][c].re, f.e[r][c].im);
+    normalize<double, true>(m);
+  }
+};
+
+// star w(x) = sum_mu U_mu(x) g^+(x+mu) + U_mu^+(x-mu) g^+(x-mu)   (overrelax.cu:350-394)
+template <typename TC, typename TSU, int NRU, typename TSG, int NRG, int NDIR>
+__device__ __forceinline__ void compute_star(const Lattice& L, const Site& c, int parity,
+                                             const typename VecOf<TSU>::type* __restrict__ U,
+                                             const typename VecOf<TSG>::type* __restrict__ G,
+                                             Mat3<TC>& star) {
+  constexpr int NCU = Field<TSU, NRU>::NCHUNK;
+  constexpr int NCG = Field<TSG, NRG>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  const int q = 1 - parity;
+  const typename VecOf<TSG>::type* Gq = G + (size_t)q * NCG * vh;
+  mzero(star);
+#pragma unroll
+  for (int mu = 0; mu < NDIR; mu++) {
+    Mat3<TC> a, b;
+    Load<TC, TSU, NRU>::go(U + (size_t)(parity * 4 + mu) * NCU * vh, vh, c.i, a);
+    const int jf = nb_fwd(L, c, mu);
+    Load<TC, TSG, NRG>::go(Gq, vh, jf, b);
+    addmul_nd(star, a, b);
+    const int jb = nb_bwd(L, c, mu);
+    Load<TC, TSU, NRU>::go(U + (size_t)(q * 4 + mu) * NCU * vh, vh, jb, a);
+    Load<TC, TSG, NRG>::go(Gq, vh, jb, b);
+    addmul_dd(star, a, b);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// overrelaxation half-sweep (overrelax.cu:335-446), in place on parity `parity`
+// ---------------------------------------------------------------------------
+template <typename T, int NRU, int NDIR>
+__global__ void __launch_bounds__(256) or_halfsweep_kernel(Lattice L,
+                                                            const typename VecOf<T>::type* U,
+                                                            typename VecOf<T>::type* G, int parity,
+                                                            T omega) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NCG = Field<T, 12>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  const Site c = site_of(L, i, parity);
+  Mat3<T> star;
+  compute_star<T, T, NRU, T, 12, NDIR>(L, c, parity, U, G, star);
+  typename VecOf<T>::type* Gp = G + (size_t)parity * NCG * vh;
+  Mat3<T> gold, g, gn;
+  Field<T, 12>::load(Gp, vh, i, gold);
+  g = gold;
+  cm_relax(g, star);
+  normalize<T, true>(g);
+  overrelax_rows01(gn, gold, g, omega);
+  Field<T, 12>::store(Gp, vh, i, gn);
+}
+
+void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
+                         int parity, double omega, int block, cudaStream_t s) {
+  dim3 grid((L.vh + block - 1) / block);
+#define OR_LAUNCH(T, NR, ND)                                                                    \
+  or_halfsweep_kernel<T, NR, ND><<<grid, block, 0, s>>>(                                     \
+      L, (const typename VecOf<T>::type*)U, (typename VecOf<T>::type*)G, parity, (T)omega)
+  if (prec == 0) {
+    if (ndir == 4) OR_LAUNCH(float, 12, 4);
+    else OR_LAUNCH(float, 12, 3);
+  } else if (link_nr == 18) {
+    if (ndir == 4) OR_LAUNCH(double, 18, 4);
+    else OR_LAUNCH(double, 18, 3);
+  } else {
+    if (ndir == 4) OR_LAUNCH(double, 12, 4);
+    else OR_LAUNCH(double, 12, 3);
+  }
+#undef OR_LAUNCH
+}
+
+// ---------------------------------------------------------------------------
+// functional and theta (overrelax.cu:451-605).
+// With X(x) = g(x) w(x) = sum_mu U'_mu(x) + U'_mu(x-mu)^+  (U' = g U g^+):
+//   sum_x Re tr X = 2 sum_{x,mu} Re tr U'_mu(x)          -> F
+//   Delta(x) = sum_mu A_mu(x-mu) - A_mu(x) = -i AH(X)     -> tr[Delta Delta^+]
+// where AH is the traceless anti-hermitian part; A = -i AH(U') is the reference's
+// vector potential.  Each block covers part of one time slice of one parity and
+// writes (sum F, sum dAdA, max dAdA).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_reduce3(double f, double d, double m, double* out) {
+  __shared__ double sh[3][32];
+  f = warp_sum(f);
+  d = warp_sum(d);
+  m = warp_max(m);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = f;
+    sh[1][w] = d;
+    sh[2][w] = m;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    f = l < nw ? sh[0][l] : 0.0;
+    d = l < nw ? sh[1][l] : 0.0;
+    m = l < nw ? sh[2][l] : 0.0;
+    f = warp_sum(f);
+    d = warp_sum(d);
+    m = warp_max(m);
+    if (l == 0) {
+      out[0] = f;
+      out[1] = d;
+      out[2] = m;
+    }
+  }
+}
+
+template <typename TC, typename TSU, int NRU, typename TSG, int NDIR>
+__global__ void __launch_bounds__(256) measure_kernel(Lattice L,
+                                                       const typename VecOf<TSU>::type* U,
+                                                       const typename VecOf<TSG>::type* G,
+                                                       double* partials) {
+  const int parity = blockIdx.z, t = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double f = 0.0, d = 0.0;
+  if (k < L.st) {
+    const int i = t * L.st + k;
+    const Site c = site_of(L, i, parity);
+    Mat3<TC> star, g;
+    compute_star<TC, TSU, NRU, TSG, 12, NDIR>(L, c, parity, U, G, star);
+    constexpr int NCG = Field<TSG, 12>::NCHUNK;
+    Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * L.vh, (size_t)L.vh, i, g);
+    Mat3<TC> X;
+    mul(X, g, star);
+    f = (double)X.e[0][0].re + (double)X.e[1][1].re + (double)X.e[2][2].re;
+    const TC tim = (X.e[0][0].im + X.e[1][1].im + X.e[2][2].im) * TC(1.0 / 3.0);
+    TC acc = TC(0);
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      const TC di = X.e[a][a].im - tim;
+      acc += di * di;
+    }
+    TC off = TC(0);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = a + 1; b < 3; b++) {
+        const TC re = (X.e[a][b].re - X.e[b][a].re) * TC(0.5);
+        const TC im = (X.e[a][b].im + X.e[b][a].im) * TC(0.5);
+        off += re * re + im * im;
+      }
+    d = (double)acc + 2.0 * (double)off;
+  }
+  const int nbx = gridDim.x;
+  block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + blockIdx.x));
+}
+
+int measure_blocks_x(const Lattice& L, int block) { return (L.st + block - 1) / block; }
+
+void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
+                    const void* G, double* partials, int block, cudaStream_t s) {
+  dim3 grid(measure_blocks_x(L, block), L.lt, 2);
+#define MEAS(TC, TSU, NR, TSG, ND)                                                    \
+  measure_kernel<TC, TSU, NR, TSG, ND><<<grid, block, 0, s>>>(                      \
+      L, (const typename VecOf<TSU>::type*)U, (const typename VecOf<TSG>::type*)G, \
+      partials)
+  if (cprec == 0) {
+    if (ndir == 4) MEAS(float, float, 12, float, 4);
+    else MEAS(float, float, 12, float, 3);
+  } else if (gprec == 0) {
+    if (link_nr == 18) {
+      if (ndir == 4) MEAS(double, double, 18, float, 4);
+      else MEAS(double, double, 18, float, 3);
+    } else {
+      if (ndir == 4) MEAS(double, double, 12, float, 4);
+      else MEAS(double, double, 12, float, 3);
+    }
+  } else {
+    if (link_nr == 18) {
+      if (ndir == 4) MEAS(double, double, 18, double, 4);
+      else MEAS(double, double, 18, double, 3);
+    } else {
+      if (ndir == 4) MEAS(double, double, 12, double, 4);
+      else MEAS(double, double, 12, double, 3);
+    }
+  }
+#undef MEAS
+}
+
+// per-slice sums: block t reduces both parities' partials of slice t (fixed order)
+__global__ void slice_reduce_kernel(const double* partials, int nbx, int lt, double* slice_sums) {
+  const int t = blockIdx.x;
+  double f = 0.0, d = 0.0, m = 0.0;
+  for (int j = threadIdx.x; j < 2 * nbx; j += blockDim.x) {
+    const int p = j / nbx, bx = j % nbx;
+    const double* q = partials + 3 * ((size_t)(p * lt + t) * nbx + bx);
+    f += q[0];
+    d += q[1];
+    m = fmax(m, q[2]);
+  }
+  block_reduce3(f, d, m, slice_sums + 3 * t);
+}
+
+enum { CRIT_MAXDADA = 0, CRIT_THETA = 1, CRIT_THETA_SLICES = 2 };
+
+__global__ void final_reduce_kernel(const double* slice_sums, int lt, double vol, double v3,
+                                    int ndir, Reduced* out, LoopState* loop, CheckRecord* hist,
+                                    int advance, cudaGraphConditionalHandle handle,
+                                    int use_handle) {
+  __shared__ double smax_theta;
+  double f = 0.0, d = 0.0, m = 0.0, tmax = 0.0;
+  for (int t = threadIdx.x; t < lt; t += blockDim.x) {
+    f += slice_sums[3 * t];
+    d += slice_sums[3 * t + 1];
+    m = fmax(m, slice_sums[3 * t + 2]);
+    tmax = fmax(tmax, slice_sums[3 * t + 1] / (3.0 * v3));
+  }
+  // one warp suffices for lt <= 32*k; reduce in a fixed order
+  __shared__ double sh[4][32];
+  f = warp_sum(f);
+  d = warp_sum(d);
+  m = warp_max(m);
+  tmax = warp_max(tmax);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = f;
+    sh[1][w] = d;
+    sh[2][w] = m;
+    sh[3][w] = tmax;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  f = d = m = tmax = 0.0;
+  for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+    f += sh[0][k];
+    d += sh[1][k];
+    m = fmax(m, sh[2][k]);
+    tmax = fmax(tmax, sh[3][k]);
+  }
+  (void)smax_theta;
+  Reduced r;
+  r.F = f / (2.0 * ndir * vol);
+  r.dAdA = d / vol;
+  r.maxdAdA = m;
+  r.theta = r.dAdA / 3.0;
+  r.theta_slice_max = tmax;
+  *out = r;
+  if (!loop) return;
+  LoopState& S = *loop;
+  S.iter += advance;
+  const double value = S.criterion == CRIT_MAXDADA ? r.maxdAdA
+                       : S.criterion == CRIT_THETA ? r.theta
+                                                   : r.theta_slice_max;
+  if (S.nhist < S.hist_cap && hist) {
+    CheckRecord& h = hist[S.nhist];
+    h.iter = S.iter;
+    h.phase = S.phase;
+    h.F = r.F;
+    h.dAdA = r.dAdA;
+    h.maxdAdA = r.maxdAdA;
+    h.theta = r.theta;
+    h.theta_slice_max = r.theta_slice_max;
+  }
+  S.nhist++;
+  S.last_F = r.F;
+  S.last_dAdA = r.dAdA;
+  S.last_max = r.maxdAdA;
+  S.last_theta = r.theta;
+  S.last_theta_slice_max = r.theta_slice_max;
+  int done = 0;
+  if (S.phase == 0) {
+    // single-precision phase: hand over to the double-precision phase when the
+    // monitored value reaches the switch threshold or stops decreasing
+    if (value < S.switch_eps || value < S.eps ||
+        (S.prev > 0.0 && value > S.plateau_ratio * S.prev))
+      done = 2;
+  } else if (value < S.eps) {
+    done = 1;
+  }
+  if (!done && S.iter + S.ck >= S.maxit) done = 3;
+  S.prev = value;
+  S.done = done;
+  if (use_handle) cudaGraphSetConditional(handle, done == 0 ? 1u : 0u);
+}
+
+void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
+                   Reduced* out, LoopState* loop, CheckRecord* hist, int advance,
+                   unsigned long long graph_handle, int use_handle, cudaStream_t s) {
+  slice_reduce_kernel<<<L.lt, 256, 0, s>>>(partials, nbx, L.lt, slice_sums);
+  const double vol = 2.0 * (double)L.vh;
+  const double v3 = (double)L.lx * L.ly * L.lz;
+  final_reduce_kernel<<<1, 256, 0, s>>>(slice_sums, L.lt, vol, v3, ndir, out, loop, hist,
+                                        advance, (cudaGraphConditionalHandle)graph_handle,
+                                        use_handle);
+}
+
+// ---------------------------------------------------------------------------
+// plaquette (overrelax.cu:34-138) and Polyakov loop
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void coords_of(const Lattice& L, int i, int parity, int& x, int& y,
+                                          int& z, int& t) {
+  Site c = site_of(L, i, parity);
+  x = 2 * c.xh + c.s;
+  y = c.y;
+  z = c.z;
+  t = c.t;
+}
+__device__ __forceinline__ int eo_of(const Lattice& L, int x, int y, int z, int t) {
+  return (x >> 1) + L.lxh * (y + L.ly * (z + L.lz * t));
+}
+__device__ __forceinline__ void shift(const Lattice& L, int mu, int dir, int& x, int& y, int& z,
+                                      int& t) {
+  if (mu == 0) x = (x + dir + L.lx) % L.lx;
+  else if (mu == 1) y = (y + dir + L.ly) % L.ly;
+  else if (mu == 2) z = (z + dir + L.lz) % L.lz;
+  else t = (t + dir + L.lt) % L.lt;
+}
+
+template <typename T, int NR>
+__device__ __forceinline__ void load_link(const Lattice& L, const typename VecOf<T>::type* U,
+                                          int x, int y, int z, int t, int mu, Mat3<double>& m) {
+  constexpr int NC = Field<T, NR>::NCHUNK;
+  const int p = (x + y + z + t) & 1;
+  Mat3<T> a;
+  Field<T, NR>::load(U + (size_t)(p * 4 + mu) * NC * L.vh, (size_t)L.vh, eo_of(L, x, y, z, t), a);
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) m.e[r][c] = cmk<double>(a.e[r][c].re, a.e[r][c].im);
+}
+
+template <typename T, int NR>
+__global__ void __launch_bounds__(256) plaquette_kernel(Lattice L, const typename VecOf<T>::type* U,
+                                                         double* partials) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (i < L.vh) {
+    int x, y, z, t;
+    coords_of(L, i, parity, x, y, z, t);
+#pragma unroll 1
+    for (int nu = 0; nu < 3; nu++)
+#pragma unroll 1
+      for (int mu = nu + 1; mu < 4; mu++) {
+        Mat3<double> M1, M2, M3, M4, A, B;
+        load_link<T, NR>(L, U, x, y, z, t, mu, M1);
+        int x1 = x, y1 = y, z1 = z, t1 = t;
+        shift(L, mu, 1, x1, y1, z1, t1);
+        load_link<T, NR>(L, U, x1, y1, z1, t1, nu, M2);
+        int x2 = x, y2 = y, z2 = z, t2 = t;
+        shift(L, nu, 1, x2, y2, z2, t2);
+        load_link<T, NR>(L, U, x2, y2, z2, t2, mu, M3);
+        load_link<T, NR>(L, U, x, y, z, t, nu, M4);
+        mul(A, M1, M2);  // U_mu(x) U_nu(x+mu)
+        mul(B, M4, M3);  // U_nu(x) U_mu(x+nu)
+        double tr = 0.0;
+#pragma unroll
+        for (int a = 0; a < 3; a++)
+#pragma unroll
+          for (int b = 0; b < 3; b++) tr += A.e[a][b].re * B.e[a][b].re + A.e[a][b].im * B.e[a][b].im;
+        acc += tr / 3.0;
+      }
+  }
+  block_reduce3(acc, 0.0, 0.0, partials + 3 * ((size_t)parity * gridDim.x + blockIdx.x));
+}
+
+__global__ void sum_partials_kernel(const double* partials, int n, double scale, double* out) {
+  double f = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) f += partials[3 * j];
+  __shared__ double sh[32];
+  f = warp_sum(f);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k];
+    *out = s * scale;
+  }
+}
+
+void launch_plaquette(int link_nr_prec, const Lattice& L, const void* U, double* partials,
+                      double* out, cudaStream_t s) {
+  const int block = 128;
+  dim3 grid((L.vh + block - 1) / block, 2);
+  if (link_nr_prec == 0)
+    plaquette_kernel<float, 12><<<grid, block, 0, s>>>(L, (const float4*)U, partials);
+  else if (link_nr_prec == 18)
+    plaquette_kernel<double, 18><<<grid, block, 0, s>>>(L, (const double2*)U, partials);
+  else
+    plaquette_kernel<double, 12><<<grid, block, 0, s>>>(L, (const double2*)U, partials);
+  const double vol = 2.0 * (double)L.vh;
+  sum_partials_kernel<<<1, 256, 0, s>>>(partials, 2 * grid.x, 1.0 / (6.0 * vol), out);
+}
+
+template <typename T, int NR>
+__global__ void polyakov_kernel(Lattice L, const typename VecOf<T>::type* U, double* partials) {
+  const int v3 = L.lx * L.ly * L.lz;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double re = 0.0, im = 0.0;
+  if (k < v3) {
+    const int x = k % L.lx, y = (k / L.lx) % L.ly, z = k / (L.lx * L.ly);
+    Mat3<double> P, U3, tmp;
+    mzero(P);
+    P.e[0][0].re = P.e[1][1].re = P.e[2][2].re = 1.0;
+    for (int t = 0; t < L.lt; t++) {
+      load_link<T, NR>(L, U, x, y, z, t, 3, U3);
+      mul(tmp, P, U3);
+      P = tmp;
+    }
+    re = (P.e[0][0].re + P.e[1][1].re + P.e[2][2].re) / 3.0;
+    im = (P.e[0][0].im + P.e[1][1].im + P.e[2][2].im) / 3.0;
+  }
+  block_reduce3(re, im, 0.0, partials + 3 * (size_t)blockIdx.x);
+}
+
+__global__ void sum_partials2_kernel(const double* partials, int n, double scale, double* out) {
+  double a = 0.0, b = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    a += partials[3 * j];
+    b += partials[3 * j + 1];
+  }
+  __shared__ double sh[2][32];
+  a = warp_sum(a);
+  b = warp_sum(b);
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = a;
+    sh[1][threadIdx.x >> 5] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s0 = 0.0, s1 = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+      s0 += sh[0][k];
+      s1 += sh[1][k];
+    }
+    out[0] = s0 * scale;
+    out[1] = s1 * scale;
+  }
+}
+
+void launch_polyakov(int link_nr_prec, const Lattice& L, const void* U, double* partials,
+                     double* out, cudaStream_t s) {
+  const int v3 = L.lx * L.ly * L.lz;
+  const int block = 128;
+  const int nb = (v3 + block - 1) / block;
+  if (link_nr_prec == 0)
+    polyakov_kernel<float, 12><<<nb, block, 0, s>>>(L, (const float4*)U, partials);
+  else if (link_nr_prec == 18)
+    polyakov_kernel<double, 18><<<nb, block, 0, s>>>(L, (const double2*)U, partials);
+  else
+    polyakov_kernel<double, 12><<<nb, block, 0, s>>>(L, (const double2*)U, partials);
+  sum_partials2_kernel<<<1, 256, 0, s>>>(partials, nb, 1.0 / (double)v3, out);
+}
+
+// ---------------------------------------------------------------------------
+// layout conversion: host AoS (su3 = complex[3][3], lexicographic, link 4*pos+mu)
+// <-> even/odd SoA planes
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long lexi_of(const Lattice& L, int i, int parity) {
+  int x, y, z, t;
+  coords_of(L, i, parity, x, y, z, t);
+  return x + (long long)L.lx * (y + (long long)L.ly * (z + (long long)L.lz * t));
+}
+
+template <typename T, int NR>
+__global__ void pack_links_kernel(Lattice L, const double* aos, typename VecOf<T>::type* U) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NC = Field<T, NR>::NCHUNK;
+  const long long pos = lexi_of(L, i, parity);
+  for (int mu = 0; mu < 4; mu++) {
+    const double* src = aos + 18 * (4 * pos + mu);
+    Mat3<T> m;
+#pragma unroll
+    for (int k = 0; k < 9; k++) m.e[k / 3][k % 3] = cmk<T>((T)src[2 * k], (T)src[2 * k + 1]);
+    Field<T, NR>::store(U + (size_t)(parity * 4 + mu) * NC * L.vh, (size_t)L.vh, i, m);
+  }
+}
+
+template <typename T, int NR>
+__global__ void unpack_links_kernel(Lattice L, const typename VecOf<T>::type* U, double* aos) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NC = Field<T, NR>::NCHUNK;
+  const long long pos = lexi_of(L, i, parity);
+  for (int mu = 0; mu < 4; mu++) {
+    Mat3<T> m;
+    Field<T, NR>::load(U + (size_t)(parity * 4 + mu) * NC * L.vh, (size_t)L.vh, i, m);
+    double* dst = aos + 18 * (4 * pos + mu);
+#pragma unroll
+    for (int k = 0; k < 9; k++) {
+      dst[2 * k] = (double)m.e[k / 3][k % 3].re;
+      dst[2 * k + 1] = (double)m.e[k / 3][k % 3].im;
+    }
+  }
+}
+
+void launch_pack_links(int link_nr_prec, const Lattice& L, const double* aos, void* U,
+                       cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (link_nr_prec == 0) pack_links_kernel<float, 12><<<grid, 128, 0, s>>>(L, aos, (float4*)U);
+  else if (link_nr_prec == 18) pack_links_kernel<double, 18><<<grid, 128, 0, s>>>(L, aos, (double2*)U);
+  else pack_links_kernel<double, 12><<<grid, 128, 0, s>>>(L, aos, (double2*)U);
+}
+void launch_unpack_links(int link_nr_prec, const Lattice& L, const void* U, double* aos,
+                         cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (link_nr_prec == 0) unpack_links_kernel<float, 12><<<grid, 128, 0, s>>>(L, (const float4*)U, aos);
+  else if (link_nr_prec == 18) unpack_links_kernel<double, 18><<<grid, 128, 0, s>>>(L, (const double2*)U, aos);
+  else unpack_links_kernel<double, 12><<<grid, 128, 0, s>>>(L, (const double2*)U, aos);
+}
+
+template <typename T>
+__global__ void pack_g_kernel(Lattice L, const double* aos, typename VecOf<T>::type* G) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NC = Field<T, 12>::NCHUNK;
+  const double* src = aos + 18 * lexi_of(L, i, parity);
+  Mat3<T> m;
+#pragma unroll
+  for (int k = 0; k < 9; k++) m.e[k / 3][k % 3] = cmk<T>((T)src[2 * k], (T)src[2 * k + 1]);
+  Field<T, 12>::store(G + (size_t)parity * NC * L.vh, (size_t)L.vh, i, m);
+}
+
+// rows 0,1 as stored; row 2 = conj(row0 x row1) as from2vtosu3_trafo (su3manip.c:303-359)
+template <typename T>
+__global__ void unpack_g_kernel(Lattice L, const typename VecOf<T>::type* G, double* aos) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NC = Field<T, 12>::NCHUNK;
+  Mat3<T> m;
+  Field<T, 12>::load(G + (size_t)parity * NC * L.vh, (size_t)L.vh, i, m);
+  Mat3<double> d;
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) d.e[r][c] = cmk<double>(m.e[r][c].re, m.e[r][c].im);
+  row2_from_01(d);
+  double* dst = aos + 18 * lexi_of(L, i, parity);
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    dst[2 * k] = d.e[k / 3][k % 3].re;
+    dst[2 * k + 1] = d.e[k / 3][k % 3].im;
+  }
+}
+
+void launch_pack_g(int gprec, const Lattice& L, const double* aos, void* G, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (gprec == 0) pack_g_kernel<float><<<grid, 128, 0, s>>>(L, aos, (float4*)G);
+  else pack_g_kernel<double><<<grid, 128, 0, s>>>(L, aos, (double2*)G);
+}
+void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (gprec == 0) unpack_g_kernel<float><<<grid, 128, 0, s>>>(L, (const float4*)G, aos);
+  else unpack_g_kernel<double><<<grid, 128, 0, s>>>(L, (const double2*)G, aos);
+}
+
+template <int NR>
+__global__ void links_64_to_32_kernel(Lattice L, const double2* U64, float4* U32) {
+  const int blk = blockIdx.y;  // parity*4 + mu
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  Mat3<double> m;
+  Field<double, NR>::load(U64 + (size_t)blk * Field<double, NR>::NCHUNK * L.vh, (size_t)L.vh, i, m);
+  Mat3<float> f;
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) f.e[r][c] = cmk<float>((float)m.e[r][c].re, (float)m.e[r][c].im);
+  Field<float, 12>::store(U32 + (size_t)blk * 3 * L.vh, (size_t)L.vh, i, f);
+}
+
+void launch_convert_links_64_to_32(int link_nr, const Lattice& L, const void* U64, void* U32,
+                                   cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 8);
+  if (link_nr == 18)
+    links_64_to_32_kernel<18><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)U32);
+  else
+    links_64_to_32_kernel<12><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)U32);
+}
+
+// g precision change; widening reunitarizes in FP64
+__global__ void g_32_to_64_kernel(Lattice L, const float4* G32, double2* G64) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  Mat3<double> m;
+  Load<double, float, 12>::go(G32 + (size_t)parity * 3 * L.vh, (size_t)L.vh, i, m);
+  Field<double, 12>::store(G64 + (size_t)parity * 6 * L.vh, (size_t)L.vh, i, m);
+}
+__global__ void g_64_to_32_kernel(Lattice L, const double2* G64, float4* G32) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  Mat3<double> m;
+  Field<double, 12>::load(G64 + (size_t)parity * 6 * L.vh, (size_t)L.vh, i, m);
+  Mat3<float> f;
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) f.e[r][c] = cmk<float>((float)m.e[r][c].re, (float)m.e[r][c].im);
+  Field<float, 12>::store(G32 + (size_t)parity * 3 * L.vh, (size_t)L.vh, i, f);
+}
+
+void launch_convert_g(int from_prec, int to_prec, const Lattice& L, const void* Gin, void* Gout,
+                      cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (from_prec == 0 && to_prec == 1)
+    g_32_to_64_kernel<<<grid, 128, 0, s>>>(L, (const float4*)Gin, (double2*)Gout);
+  else if (from_prec == 1 && to_prec == 0)
+    g_64_to_32_kernel<<<grid, 128, 0, s>>>(L, (const double2*)Gin, (float4*)Gout);
+}
+
+// U_mu(x) <- g(x) U_mu(x) g^+(x+mu), in place, FP64 (the host g_trafo of
+// observables.c:17-47 moved to the device)
+template <int NR>
+__global__ void apply_trafo_kernel(Lattice L, double2* U, const double2* G) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  constexpr int NC = Field<double, NR>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  const Site c = site_of(L, i, parity);
+  Mat3<double> g, gn, u, h, r;
+  Field<double, 12>::load(G + (size_t)parity * 6 * vh, vh, i, g);
+  for (int mu = 0; mu < 4; mu++) {
+    double2* blk = U + (size_t)(parity * 4 + mu) * NC * vh;
+    Field<double, NR>::load(blk, vh, i, u);
+    Field<double, 12>::load(G + (size_t)(1 - parity) * 6 * vh, vh, nb_fwd(L, c, mu), gn);
+    mul(h, g, u);
+    mzero(r);
+    addmul_nd(r, h, gn);
+    Field<double, NR>::store(blk, vh, i, r);
+  }
+}
+
+void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  if (link_nr == 18)
+    apply_trafo_kernel<18><<<grid, 128, 0, s>>>(L, (double2*)U64, (const double2*)G64);
+  else
+    apply_trafo_kernel<12><<<grid, 128, 0, s>>>(L, (double2*)U64, (const double2*)G64);
+}
+
+}  // namespace gfx

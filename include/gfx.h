@@ -1,0 +1,210 @@
+/*
+ * gfx.h -- C ABI of libgfx, the sm_103a (GB300) implementation of the cudagfx
+ * gauge-fixing hot path.
+ *
+ * Two layers are exported:
+ *   1. gfx_* : explicit-argument, context-handle functions returning gfx_status.
+ *   2. the reference's own entry points (init_gaugefixing, overrelax_gauge,
+ *      calc_functional, ...) with the reference's global variables, declared in
+ *      gfx_legacy.h, so the reference's C host code links against libgfx unchanged.
+ *
+ * Conventions shared with the reference host code:
+ *   - a site is pos = x + LX*(y + LY*(z + LZ*t)) (cudagaugefix.cu:79); directions
+ *     mu = 0,1,2,3 = x,y,z,t;
+ *   - host matrices are su3 = complex[3][3] of doubles, row-major, (re, im)
+ *     interleaved: 18 doubles (global.h:26-33);
+ *   - a gauge field is 4*V su3 with link (pos, mu) at index 4*pos+mu; a gauge
+ *     transformation is V su3 with g(pos) at index pos.
+ * All pointers are host pointers unless the name ends in _device.  No call keeps
+ * a host pointer after it returns.
+ */
+#ifndef GFX_H
+#define GFX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFX_ABI_VERSION 1
+
+typedef enum {
+  GFX_OK = 0,
+  GFX_ERR_BAD_VOLUME = 1,    /* extents not even / volume not supported (reference: exit(100)) */
+  GFX_ERR_OOM = 2,           /* device allocation failed (reference: exit(200)) */
+  GFX_ERR_NOT_CONVERGED = 3, /* iteration cap reached (reference: overrelax_gauge returns -1) */
+  GFX_ERR_IO = 4,            /* file missing, truncated or malformed (reference: exit(400)) */
+  GFX_ERR_CUDA = 5,          /* a CUDA runtime call failed */
+  GFX_ERR_ARG = 6,           /* invalid argument */
+  GFX_ERR_STATE = 7          /* call out of order (e.g. update before init) */
+} gfx_status;
+
+typedef enum { GFX_PREC_DOUBLE = 0, GFX_PREC_SINGLE = 1, GFX_PREC_MIXED = 2 } gfx_precision;
+typedef enum { GFX_GAUGE_LANDAU = 0, GFX_GAUGE_COULOMB = 1 } gfx_gauge;
+typedef enum {
+  GFX_CRIT_MAXDADA = 0,     /* max_x tr[Delta Delta^+] < eps (the reference criterion, overrelax.cu:794) */
+  GFX_CRIT_THETA = 1,       /* theta = (1/3V) sum_x tr[Delta Delta^+] < eps */
+  GFX_CRIT_THETA_SLICES = 2 /* max over time slices of theta_t < eps (Coulomb gauge) */
+} gfx_criterion;
+
+typedef struct gfx_ctx gfx_ctx;
+
+/* calc_functional's results (overrelax.cu:610-671) plus theta */
+typedef struct {
+  double F;               /* (1/(ndir V)) sum_{x,mu} Re tr g(x) U_mu(x) g^+(x+mu) */
+  double dAdA;            /* (1/V) sum_x tr[Delta Delta^+] */
+  double maxdAdA;         /* max_x tr[Delta Delta^+] */
+  double theta;           /* dAdA / 3 */
+  double theta_slice_max; /* max_t (1/(3 V3)) sum_{x in slice t} tr[Delta Delta^+] */
+} gfx_functional_t;
+
+typedef struct {
+  int maxit;              /* iteration cap (overrelax_gauge's maxit) */
+  double eps;             /* convergence threshold on the criterion */
+  int checkinterval;      /* sweeps between functional evaluations */
+  double omega;           /* overrelaxation parameter (reference: 1.68, overrelax.cu:416) */
+  int criterion;          /* gfx_criterion */
+  int gauge;              /* gfx_gauge */
+  double switch_eps;      /* mixed: leave the FP32 phase when its value drops below this */
+  double plateau_ratio;   /* mixed: ... or when value_new > plateau_ratio * value_old */
+  int checkinterval_double; /* sweeps between checks in the FP64 phase (0: checkinterval) */
+  int use_graph;          /* 1: device-side loop in a CUDA graph (conditional while node) */
+  int record_history;     /* keep every check (gfx_or_history) */
+} gfx_or_params;
+
+typedef struct {
+  int iterations;     /* overrelax_gauge's return value: iteration of the converging check, or -1 */
+  int sweeps;         /* sweeps performed */
+  int sweeps_single;  /* of which in FP32 */
+  int sweeps_double;  /* of which in FP64 */
+  int converged;
+  int checks;         /* functional evaluations */
+  gfx_functional_t final_values; /* last evaluation (FP64 unless precision is SINGLE) */
+  double ms;          /* device time of the whole call (CUDA events) */
+} gfx_or_result;
+
+typedef struct {
+  int iter;
+  int phase; /* 0: FP32 sweeps, 1: FP64 (or final) sweeps */
+  double F, dAdA, maxdAdA, theta, theta_slice_max;
+} gfx_check_record;
+
+/* SAPARAM_LIST (global.h:51-57) plus the number of microcanonical sweeps per step */
+typedef struct {
+  double Tmin, Tmax, expo;
+  int N;
+  int checkint;
+  int nmicro;
+} gfx_sa_params;
+
+typedef struct {
+  int Nsweep;
+  int checkint;
+  double beta;
+} gfx_therm_params;
+
+/* ---- library / context ---- */
+int gfx_abi_version(void);
+const char *gfx_status_string(int status);
+/* last error message of this context (or the global one when ctx is NULL) */
+const char *gfx_last_error(const gfx_ctx *ctx);
+
+/* Create a context on the current device.  link_reals64 = 12 (two-row storage,
+ * the reference layout) or 18 (full matrices) for the FP64 link copy.
+ * stream = a cudaStream_t to run on, or NULL for a private stream. */
+gfx_status gfx_create(gfx_ctx **out, int lx, int ly, int lz, int lt, int precision,
+                      int link_reals64, void *stream);
+gfx_status gfx_destroy(gfx_ctx *ctx);
+gfx_status gfx_synchronize(gfx_ctx *ctx);
+/* bytes of device memory held by the context */
+size_t gfx_device_bytes(const gfx_ctx *ctx);
+/* threads per block of the sweep kernels (0: library default / autotuned) */
+gfx_status gfx_set_block(gfx_ctx *ctx, int block);
+
+/* ---- fields (init_gaugefixing / gfx_get_trafo of the reference's main, cudagaugefix.cu:204-374, 785-793) ---- */
+gfx_status gfx_set_links(gfx_ctx *ctx, const double *su3_links);
+gfx_status gfx_get_links(gfx_ctx *ctx, double *su3_links);
+gfx_status gfx_set_trafo(gfx_ctx *ctx, const double *su3_trafo);
+gfx_status gfx_get_trafo(gfx_ctx *ctx, double *su3_trafo);
+/* g <- 1 */
+gfx_status gfx_unit_trafo(gfx_ctx *ctx);
+
+/* ---- gauge fixing ---- */
+void gfx_or_params_default(gfx_or_params *p);
+/* overrelax_gauge (overrelax.cu:677-823) */
+gfx_status gfx_overrelax(gfx_ctx *ctx, const gfx_or_params *p, gfx_or_result *res);
+/* copy up to cap check records of the last gfx_overrelax call; returns the count */
+int gfx_or_history(const gfx_ctx *ctx, gfx_check_record *out, int cap);
+/* nsweeps plain OR sweeps (even then odd) without checks; precision 0 = FP32, 1 = FP64 */
+gfx_status gfx_or_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision);
+/* one OR half-sweep of one parity */
+gfx_status gfx_or_halfsweep(gfx_ctx *ctx, int parity, double omega, int gauge, int precision);
+/* calc_functional (overrelax.cu:610-671); precision 0 = FP32 arithmetic, 1 = FP64 */
+gfx_status gfx_functional(gfx_ctx *ctx, int gauge, int precision, gfx_functional_t *out);
+/* calc_plaquette (overrelax.cu:115-138) on the links */
+gfx_status gfx_plaquette(gfx_ctx *ctx, double *plaq);
+/* Polyakov loop (1/V3) sum_xvec tr prod_t U_t / 3 -> re_im[2] */
+gfx_status gfx_polyakov(gfx_ctx *ctx, double *re_im);
+/* U_mu(x) <- g(x) U_mu(x) g^+(x+mu) on the device, then g <- 1
+ * (dev_apply_trafo overrelax.cu:273-331 / g_trafo observables.c:17-47) */
+gfx_status gfx_apply_trafo(gfx_ctx *ctx);
+
+/* device time (CUDA events on the context's stream) of nsweeps plain OR sweeps */
+gfx_status gfx_time_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision,
+                           double *ms);
+/* number of kernels this context has enqueued (graph bodies counted per execution) */
+unsigned long long gfx_launch_count(const gfx_ctx *ctx);
+
+/* ---- Mersenne Twister bank (MersenneTwister.cu / .h) ---- */
+/* params: 4096 records {matrix_a, mask_b, mask_c, seed}, the MersenneTwister.dat layout */
+gfx_status gfx_mt_load_params(gfx_ctx *ctx, const uint32_t *params);
+gfx_status gfx_mt_load_file(gfx_ctx *ctx, const char *path);
+/* seedMTGPU with srand(mtseed): seed_i = i-th rand() (MersenneTwister.cu:98-114) */
+gfx_status gfx_mt_seed(gfx_ctx *ctx, unsigned int mtseed);
+gfx_status gfx_mt_set_seeds(gfx_ctx *ctx, const uint32_t *seeds);
+/* init_MT (MersenneTwister.cu:236-289) */
+gfx_status gfx_mt_init(gfx_ctx *ctx, int n_gauss, int n_unif);
+/* update_MT (MersenneTwister.cu:295-323) */
+gfx_status gfx_mt_update(gfx_ctx *ctx);
+/* read the current fields (sizes 4096*nper) and, optionally, the state [19][4096] and seeds[4096] */
+gfx_status gfx_mt_read(gfx_ctx *ctx, float *gauss, float *unif, uint32_t *state, uint32_t *seeds);
+gfx_status gfx_mt_sizes(const gfx_ctx *ctx, int *nper_gauss, int *nper_unif);
+
+/* ---- simulated annealing (simulated_annealing.cu) ---- */
+/* set_sa_temperature (simulated_annealing.cu:265-299) */
+double gfx_sa_temperature(const gfx_sa_params *p, int i);
+/* simannealing_gauge (simulated_annealing.cu:309-476), plus p->nmicro microcanonical
+ * sweeps per heatbath step; needs an initialized MT bank */
+gfx_status gfx_simanneal(gfx_ctx *ctx, const gfx_sa_params *p, gfx_functional_t *last);
+/* steps first .. first+count-1 of the schedule (for callers that check in between) */
+gfx_status gfx_simanneal_range(gfx_ctx *ctx, const gfx_sa_params *p, int first, int count);
+/* single half-sweeps with the current random fields */
+gfx_status gfx_sa_halfsweep(gfx_ctx *ctx, int parity, double beta, int precision);
+gfx_status gfx_micro_halfsweep(gfx_ctx *ctx, int parity, int gauge, int precision);
+
+/* ---- thermalization (heatbath_thermalization.cu) ---- */
+/* thermalize_gauge (heatbath_thermalization.cu:568-841): Nsweep x 4 directions x 2 parities,
+ * beta/3 per set_beta; plaquette every checkint sweeps into plaq (if non-NULL, capacity
+ * Nsweep/checkint + 1).  The result stays on the device (gfx_get_links). */
+gfx_status gfx_thermalize(gfx_ctx *ctx, const gfx_therm_params *p, double *plaq, int plaq_cap);
+gfx_status gfx_link_heatbath_halfsweep(gfx_ctx *ctx, int parity, int nu, double beta);
+
+/* ---- host-side helpers ---- */
+/* page-locked host memory for the field copies (cudaMallocHost); NULL on failure */
+void *gfx_host_alloc(size_t bytes);
+void gfx_host_free(void *p);
+/* glibc srand(seed)/rand() stream */
+void gfx_glibc_rand(unsigned int seed, int n, int32_t *out);
+/* random_init_trafo / random_init_gauge with Park-Miller PlantSeeds(seed) (su3manip.c:539-767) */
+void gfx_random_init_reference(long seed, double *su3, long n);
+/* Haar-distributed SU(3) matrices from a seeded counter-based generator */
+void gfx_random_init_haar(uint64_t seed, double *su3, long n);
+/* unit matrices */
+void gfx_unit_init(double *su3, long n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,78 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+  oracle/liboracle.so        the CPU restatement in gfx_oracle.c (gcc, -ffp-contract=off)
+  oracle/_ref/libref_host.so the reference's own host C files -- su3manip.c,
+                             observables.c, rngs.c, complex.c -- compiled where they
+                             lie in the reference checkout (only when it is present),
+                             plus ref_globals.c which defines the globals the
+                             reference's main would define.
+  oracle/_ref/MersenneTwister.dat   the reference's twister-parameter file, copied
+                             next to the reference build so that tests can load it.
+
+Nothing here is part of the product; only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg use it.
+"""
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+ORACLE_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(REF_DIR, "libref_host.so")
+REF_DAT = os.path.join(REF_DIR, "MersenneTwister.dat")
+REFERENCE = os.environ.get("GFX_REFERENCE_DIR", "/root/reference")
+REF_SOURCES = ["su3manip.c", "observables.c", "rngs.c", "complex.c"]
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("%s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _newer(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def build_oracle():
+    src = os.path.join(HERE, "gfx_oracle.c")
+    if _newer(ORACLE_LIB, [src, os.path.join(HERE, "gfx_oracle.h"), __file__]):
+        _run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", "-std=c99",
+              src, "-o", ORACLE_LIB, "-lm"])
+    return ORACLE_LIB
+
+
+def reference_present():
+    return all(os.path.exists(os.path.join(REFERENCE, f)) for f in REF_SOURCES + ["global.h"])
+
+
+def build_reference_host():
+    """Compile the reference's host observables/initializers; None if the reference
+    checkout is not present (as on a machine that only has this repository)."""
+    if not reference_present():
+        return REF_LIB if os.path.exists(REF_LIB) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    srcs = [os.path.join(REFERENCE, f) for f in REF_SOURCES]
+    glob = os.path.join(HERE, "ref_globals.c")
+    if _newer(REF_LIB, srcs + [glob, __file__]):
+        cuda_inc = "/usr/local/cuda/include"
+        _run(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC", "-w",
+              "-I" + REFERENCE, "-I" + cuda_inc] + srcs + [glob, "-o", REF_LIB, "-lm"])
+    dat = os.path.join(REFERENCE, "MersenneTwister.dat")
+    if os.path.exists(dat) and _newer(REF_DAT, [dat]):
+        shutil.copyfile(dat, REF_DAT)
+    return REF_LIB
+
+
+def build():
+    build_oracle()
+    build_reference_host()
+
+
+if __name__ == "__main__":
+    build()
+    print(ORACLE_LIB, REF_LIB if os.path.exists(REF_LIB) else "(reference not built)")

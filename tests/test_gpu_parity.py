@@ -1,0 +1,348 @@
+"""GPU parity of the sm_103a kernels (called through the C ABI of libgfx.so) against
+the CPU oracle, on seeded small lattices.  Tolerances are stated per test."""
+import numpy as np
+import pytest
+
+from conftest import haar, smooth_links
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (8, 8, 8, 8)
+DIMS_ODD_SHAPE = (4, 6, 8, 10)
+
+
+def _ctx(gfx, dims, prec=0, link_reals=12):
+    return gfx.Context(dims, precision=prec, link_reals=link_reals)
+
+
+def _setup(gfx, oracle, dims, seed, prec=0, link_reals=12, eps=0.35):
+    u = smooth_links(dims, eps, seed)
+    g = haar(int(np.prod(dims)), seed + 1)
+    ctx = _ctx(gfx, dims, prec, link_reals)
+    ctx.set_links(u)
+    ctx.set_trafo(g)
+    lat = oracle.lattice(dims)
+    return ctx, lat, u, g
+
+
+def _g12(g18):
+    return np.ascontiguousarray(np.asarray(g18).reshape(-1, 18)[:, :12])
+
+
+@pytest.mark.parametrize("dims", [DIMS, DIMS_ODD_SHAPE])
+def test_fields_roundtrip(gfx, oracle, dims):
+    ctx, lat, u, g = _setup(gfx, oracle, dims, 1)
+    assert np.array_equal(ctx.get_links().reshape(-1, 18), u)
+    got = ctx.get_trafo().reshape(-1, 18)
+    assert np.array_equal(got[:, :12], g[:, :12])
+    assert np.max(np.abs(got - oracle.from2v(_g12(g)))) < 1e-15
+
+
+@pytest.mark.parametrize("link_reals", [12, 18])
+@pytest.mark.parametrize("dims", [DIMS, DIMS_ODD_SHAPE])
+def test_or_halfsweep_fp64(gfx, oracle, dims, link_reals):
+    """One even and one odd half-sweep: g agrees with the oracle to 1e-13."""
+    ctx, lat, u, g = _setup(gfx, oracle, dims, 3, link_reals=link_reals)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    for parity in (0, 1):
+        ctx.or_halfsweep(parity, omega=1.68, precision=1)
+        oracle.or_halfsweep(lat, gf12, g12, parity, 1.68)
+        got = _g12(ctx.get_trafo())
+        assert np.max(np.abs(got - g12)) < 1e-13
+
+
+def test_or_sweeps_fp64_track_oracle(gfx, oracle):
+    """30 sweeps: the functional and dAdA follow the oracle (relative 1e-12 on F,
+    1e-9 on dAdA)."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 5)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    for _ in range(3):
+        ctx.or_sweeps(10, omega=1.68, precision=1)
+        oracle.or_sweeps(lat, gf12, g12, 10, 1.68)
+        f = ctx.functional(precision=1)
+        o = oracle.functional(lat, gf12, g12)
+        assert f.F == pytest.approx(o["F"], rel=1e-12)
+        assert f.dAdA == pytest.approx(o["dAdA"], rel=1e-9)
+        assert f.maxdAdA == pytest.approx(o["maxdAdA"], rel=1e-9)
+
+
+@pytest.mark.parametrize("dims", [DIMS, DIMS_ODD_SHAPE])
+def test_functional_fp64(gfx, oracle, dims):
+    ctx, lat, u, g = _setup(gfx, oracle, dims, 7, eps=0.6)
+    f = ctx.functional(precision=1)
+    o = oracle.functional(lat, oracle.to2v(u), _g12(g))
+    assert f.F == pytest.approx(o["F"], rel=1e-13)
+    assert f.dAdA == pytest.approx(o["dAdA"], rel=1e-12)
+    assert f.maxdAdA == pytest.approx(o["maxdAdA"], rel=1e-12)
+    assert f.theta == pytest.approx(o["dAdA"] / 3, rel=1e-12)
+
+
+def test_functional_fp32(gfx, oracle):
+    """FP32 arithmetic on FP32-stored fields, FP64 accumulation: relative 1e-5."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 9, prec=2, eps=0.6)
+    f = ctx.functional(precision=0)
+    o = oracle.functional(lat, oracle.to2v(u), _g12(g))
+    assert f.F == pytest.approx(o["F"], rel=1e-5)
+    assert f.dAdA == pytest.approx(o["dAdA"], rel=1e-4)
+
+
+def test_or_halfsweep_fp32(gfx, oracle):
+    """FP32 sweep vs FP64 oracle: g within 2e-5 after one sweep."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 11, prec=2)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    ctx.or_sweeps(1, omega=1.68, precision=0)
+    oracle.or_sweeps(lat, gf12, g12, 1, 1.68)
+    got = _g12(ctx.get_trafo())
+    assert np.max(np.abs(got - g12)) < 2e-5
+
+
+@pytest.mark.parametrize("dims", [DIMS, DIMS_ODD_SHAPE])
+def test_plaquette_and_polyakov(gfx, oracle, dims):
+    ctx, lat, u, g = _setup(gfx, oracle, dims, 13, eps=0.7)
+    gf12 = oracle.to2v(u)
+    assert ctx.plaquette() == pytest.approx(oracle.plaquette(lat, gf12), rel=1e-14)
+    p = ctx.polyakov()
+    q = oracle.polyakov(lat, gf12)
+    assert abs(p - q) < 1e-13
+
+
+def test_apply_trafo_matches_oracle_and_keeps_invariants(gfx, oracle):
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 15, eps=0.7)
+    p0, l0 = ctx.plaquette(), ctx.polyakov()
+    ctx.apply_trafo()
+    want = oracle.g_trafo18(lat, u, oracle.from2v(_g12(g)))
+    got = ctx.get_links().reshape(-1, 18)
+    assert np.max(np.abs(got[:, :12] - want[:, :12])) < 1e-13
+    assert ctx.plaquette() == pytest.approx(p0, rel=1e-12)
+    assert abs(ctx.polyakov() - l0) < 1e-12
+    # g was reset to the identity
+    assert np.max(np.abs(ctx.get_trafo().reshape(-1, 18) - np.tile(
+        [1, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 1, 0], (512 * 8, 1)))) == 0
+
+
+def _oracle_overrelax(oracle, lat, gf12, g12, maxit, eps, ck, omega, key="maxdAdA", ndir=4):
+    last = 0.0
+    for i in range(maxit):
+        oracle.or_halfsweep(lat, gf12, g12, 0, omega, ndir)
+        oracle.or_halfsweep(lat, gf12, g12, 1, omega, ndir)
+        if i % ck == 0:
+            f = oracle.functional(lat, gf12, g12, ndir)
+            last = f[key] if key != "theta" else f["dAdA"] / 3
+        if last < eps:
+            return i, f
+    return -1, f
+
+
+@pytest.mark.parametrize("use_graph", [1, 0])
+def test_overrelax_gauge_fp64_matches_oracle(gfx, oracle, use_graph):
+    """overrelax_gauge semantics: the same converging check iteration as the oracle,
+    and the final functional to 1e-12."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 17)
+    r = ctx.overrelax(maxit=3000, eps=1e-10, checkinterval=10, omega=1.68, use_graph=use_graph)
+    it, f = _oracle_overrelax(oracle, lat, oracle.to2v(u), _g12(g), 3000, 1e-10, 10, 1.68)
+    assert r.converged == 1
+    assert r.iterations == it
+    assert r.sweeps == it + 1
+    assert r.final_values.F == pytest.approx(f["F"], rel=1e-12)
+    assert r.final_values.maxdAdA < 1e-10
+    hist = ctx.history()
+    assert [h["iter"] for h in hist] == list(range(0, it + 1, 10))
+
+
+def test_overrelax_not_converged_returns_minus_one(gfx, oracle):
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 19)
+    r = ctx.overrelax(maxit=25, eps=1e-30, checkinterval=10)
+    assert r.converged == 0
+    assert r.iterations == -1
+    assert r.sweeps == 25
+
+
+def test_mixed_precision_reaches_theta(gfx, oracle):
+    """Mixed FP32 -> FP64: converges to theta < 1e-12 verified in FP64, and lands on
+    the same functional as the all-FP64 path (relative 1e-9)."""
+    u = smooth_links(DIMS, 0.35, 21)
+    g = haar(4096, 22)
+    res = {}
+    for prec in (0, 2):
+        ctx = gfx.Context(DIMS, precision=prec)
+        ctx.set_links(u)
+        ctx.set_trafo(g)
+        r = ctx.overrelax(maxit=5000, eps=1e-12, checkinterval=20, omega=1.7,
+                          criterion=gfx.CRIT_THETA, switch_eps=1e-9)
+        assert r.converged == 1
+        f = ctx.functional(precision=1)
+        assert f.theta < 1e-12
+        res[prec] = (r, f)
+    assert res[2][1].F == pytest.approx(res[0][1].F, rel=1e-9)
+    assert res[2][0].sweeps_single > 0
+
+
+def test_coulomb_functional_and_convergence(gfx, oracle):
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS_ODD_SHAPE, 23, eps=0.5)
+    f = ctx.functional(gauge=gfx.COULOMB, precision=1)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    o = oracle.functional(lat, gf12, g12, ndir=3)
+    th = oracle.theta_slices(lat, gf12, g12, ndir=3)
+    assert f.F == pytest.approx(o["F"], rel=1e-13)
+    assert f.dAdA == pytest.approx(o["dAdA"], rel=1e-12)
+    assert f.theta_slice_max == pytest.approx(th.max(), rel=1e-12)
+    r = ctx.overrelax(maxit=4000, eps=1e-13, checkinterval=20, omega=1.7, gauge=gfx.COULOMB,
+                      criterion=gfx.CRIT_THETA_SLICES)
+    assert r.converged == 1
+    th = oracle.theta_slices(lat, gf12, _g12(ctx.get_trafo()), ndir=3)
+    assert th.max() < 1e-13
+    # the temporal links are untouched by the gauge condition; the plaquette is invariant
+    assert ctx.plaquette() == pytest.approx(oracle.plaquette(lat, gf12), rel=1e-14)
+
+
+# ----------------------------------------------------------------------------
+# Mersenne Twister bank
+# ----------------------------------------------------------------------------
+def _mt_ctx(gfx, mt_params, seed, ng, nu, dims=(4, 4, 4, 4)):
+    ctx = gfx.Context(dims)
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(seed)
+    ctx.mt_init(ng, nu)
+    return ctx
+
+
+@pytest.mark.parametrize("ng,nu", [(4096 * 38, 4096 * 19), (4096 * 6, 4096 * 24), (5000, 70001)])
+def test_mt_bank_bit_exact(gfx, oracle, mt_params, ng, nu):
+    """Uniform fields and the twister state are bit-exact with the oracle through init
+    and three updates; gaussians (fast-math Box-Muller) agree to 2e-4 absolute."""
+    ctx = _mt_ctx(gfx, mt_params, 1234, ng, nu)
+    npg, npu = ctx.mt_sizes()
+    assert (npg, npu) == (oracle.mt_nper(ng), oracle.mt_nper(nu))
+    seeds = gfx.glibc_rand(1234, 4096).astype(np.uint32)
+    m = oracle.mt_new(mt_params, seeds=seeds)
+    og, ou = oracle.mt_init_fields(m, npg, npu)
+    for step in range(4):
+        g, u, st, sd = ctx.mt_read()
+        assert np.array_equal(u, ou), step
+        assert np.array_equal(st.T.reshape(-1), np.ctypeslib.as_array(m.status)), step
+        assert np.array_equal(sd, np.ctypeslib.as_array(m.seed)), step
+        assert np.max(np.abs(g - og)) < 2e-4, step
+        ctx.mt_update()
+        og, ou = oracle.mt_update_fields(m, npg, npu)
+
+
+def test_mt_uniform_range_and_moments(gfx, mt_params):
+    ctx = _mt_ctx(gfx, mt_params, 99, 4096 * 64, 4096 * 64)
+    g, u, _, _ = ctx.mt_read()
+    assert u.min() > 0.0 and u.max() <= 1.0
+    assert abs(u.mean() - 0.5) < 5e-3
+    assert abs(g.mean()) < 1e-2 and abs(g.std() - 1.0) < 1e-2
+
+
+# ----------------------------------------------------------------------------
+# heatbath family
+# ----------------------------------------------------------------------------
+def test_sa_heatbath_halfsweep_matches_oracle(gfx, oracle, mt_params):
+    """Same random fields: all but a few sites (accept/reject decisions at the single-
+    precision boundary) agree to 1e-12."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 25)
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(7)
+    V = 4096
+    ctx.mt_init(V // 2, 2 * V)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    for parity, beta in ((0, 1.0 / 1.45), (1, 1.0 / 0.3)):
+        gs, us, _, _ = ctx.mt_read()
+        ctx.sa_halfsweep(parity, beta, precision=1)
+        oracle.heatbath_halfsweep(lat, gf12, g12, parity, gs, us, beta)
+        got = _g12(ctx.get_trafo())
+        bad = np.max(np.abs(got - g12), axis=1) > 1e-12
+        assert bad.sum() <= 4, bad.sum()
+        g12[bad] = got[bad]
+        ctx.mt_update()
+
+
+def test_micro_halfsweep_matches_oracle_and_keeps_functional(gfx, oracle):
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 27)
+    gf12, g12 = oracle.to2v(u), _g12(g)
+    f0 = ctx.functional(precision=1).F
+    for parity in (0, 1):
+        ctx.micro_halfsweep(parity, precision=1)
+        oracle.micro_halfsweep(lat, gf12, g12, parity)
+    assert np.max(np.abs(_g12(ctx.get_trafo()) - g12)) < 1e-13
+    assert ctx.functional(precision=1).F == pytest.approx(f0, rel=1e-12)
+
+
+def test_link_heatbath_halfsweep_matches_oracle(gfx, oracle, mt_params):
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 29, eps=0.5)
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(11)
+    V = 4096
+    ctx.mt_init(2 * V, 8 * V)
+    gf12 = oracle.to2v(u)
+    for parity, nu in ((0, 0), (1, 0), (0, 3), (1, 2)):
+        gs, us, _, _ = ctx.mt_read()
+        ctx.link_heatbath_halfsweep(parity, nu, 6.0)
+        oracle.link_heatbath_halfsweep(lat, gf12, parity, nu, gs, us, 6.0)
+        got = oracle.to2v(ctx.get_links())
+        bad = np.max(np.abs(got - gf12), axis=1) > 1e-12
+        assert bad.sum() <= 4, bad.sum()
+        gf12[bad] = got[bad]
+        ctx.mt_update()
+
+
+def test_thermalization_moves_plaquette(gfx, mt_params):
+    ctx = gfx.Context(DIMS)
+    ctx.set_links(gfx.unit_init(4 * 4096))
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(1234)
+    ctx.mt_init(2 * 4096, 8 * 4096)
+    plaq = ctx.thermalize(6.0, 20, checkint=5)
+    assert len(plaq) == 4
+    assert plaq[0] < 1.0 and 0.0 < plaq[-1] < plaq[0]
+    # links stay in SU(3)
+    u = ctx.get_links().reshape(-1, 3, 3, 2)
+    m = u[..., 0] + 1j * u[..., 1]
+    assert np.max(np.abs(m @ np.conj(np.swapaxes(m, 1, 2)) - np.eye(3))) < 1e-12
+
+
+def test_simanneal_then_overrelax(gfx, oracle, mt_params):
+    """SA (2 x 50 steps, 3 micro per step) then OR: reaches theta < 1e-12."""
+    ctx, lat, u, g = _setup(gfx, oracle, DIMS, 31, prec=2)
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(7)
+    ctx.mt_init(4096 // 2, 2 * 4096)
+    f0 = ctx.functional(precision=1)
+    f1 = ctx.simanneal(0.01, 1.45, 100, expo=-1.0, nmicro=3)
+    assert f1.F > f0.F
+    r = ctx.overrelax(maxit=5000, eps=1e-12, checkinterval=20, omega=1.7,
+                      criterion=gfx.CRIT_THETA, switch_eps=1e-9)
+    assert r.converged == 1
+
+
+def test_sa_temperature_schedules(gfx):
+    from cudagfx_gb300 import sa_temperature
+    assert sa_temperature(0.01, 1.45, 2000, -1.0, 0) == pytest.approx(1.45)
+    assert sa_temperature(0.01, 1.45, 2000, -1.0, 1999) == pytest.approx(0.01)
+    assert sa_temperature(0.01, 1.45, 100, 0.0, 99) == pytest.approx(0.01)
+    assert sa_temperature(0.01, 1.45, 100, 2.0, 99) == pytest.approx(0.01)
+
+
+# ----------------------------------------------------------------------------
+# reference-named entry points
+# ----------------------------------------------------------------------------
+def test_legacy_entry_points(gfx, oracle):
+    from cudagfx_gb300 import legacy
+    u = smooth_links(DIMS, 0.35, 33)
+    g = haar(4096, 34)
+    legacy.set_lattice(*DIMS)
+    legacy.set_precision(gfx.PREC_DOUBLE)
+    legacy.init_gaugefixing(u, g)
+    m = legacy.calc_functional()
+    lat = oracle.lattice(DIMS)
+    o = oracle.functional(lat, oracle.to2v(u), _g12(g))
+    assert m == pytest.approx(o["maxdAdA"], rel=1e-12)
+    assert legacy.gvar("FUNC").value == pytest.approx(o["F"], rel=1e-13)
+    assert legacy.calc_plaquette(0) == pytest.approx(oracle.plaquette(lat, oracle.to2v(u)),
+                                                     rel=1e-14)
+    it = legacy.overrelax_gauge(3000, 1e-10, 10)
+    assert it >= 0 and it % 10 == 0
+    assert legacy.gvar("maxDADA").value < 1e-10
+    t = legacy.get_trafo()
+    assert t.shape == (4096, 3, 3, 2)
+    legacy.finalize_gaugefixing()
