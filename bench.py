@@ -51,12 +51,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gfx", choices=["gfx", "reference"])
     ap.add_argument("--dims", default="32,32,32,32")
-    ap.add_argument("--therm", type=int, default=50, help="heatbath sweeps for the links")
+    ap.add_argument("--therm", type=int, default=200, help="heatbath sweeps for the links")
     ap.add_argument("--beta", type=float, default=6.0)
     ap.add_argument("--eps", type=float, default=1e-12)
     ap.add_argument("--omega", type=float, default=1.7)
     ap.add_argument("--checkinterval", type=int, default=25)
-    ap.add_argument("--switch-eps", type=float, default=0.0)
+    ap.add_argument("--switch-eps", type=float, default=1e-10)
+    ap.add_argument("--checkinterval-double", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
     ap.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample sweeps (0: auto)")
     return ap.parse_args()
@@ -257,14 +258,15 @@ def run_gfx(args, dims):
     ctx.mt_seed(42 + rank)
     ctx.mt_init(2 * V, 8 * V)
     t0 = time.perf_counter()
-    ctx.thermalize(args.beta, args.therm)
+    ctx.thermalize(args.beta, args.therm, variant=gfx.HB_KENNEDY_PENDLETON)
     therm_s = time.perf_counter() - t0
     plaq = ctx.plaquette()
     links = ctx.get_links()
     g0 = gfx.random_init_reference(351 + rank, V)
     params = ctx.or_params(maxit=200000, eps=args.eps, checkinterval=args.checkinterval,
                            omega=args.omega, criterion=gfx.CRIT_THETA,
-                           switch_eps=args.switch_eps, checkinterval_double=args.checkinterval)
+                           switch_eps=args.switch_eps,
+                           checkinterval_double=args.checkinterval_double)
 
     def solve(c):
         c.set_trafo(g0)
@@ -355,8 +357,9 @@ def run_gfx(args, dims):
         "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
         "config": {
-            "workload": "%s Landau gauge fixing: beta=%g heatbath links (%d sweeps from cold, MT "
-                        "seed 42), reference random gauge start (RandSeed 351), mixed FP32->FP64 "
+            "workload": "%s Landau gauge fixing: beta=%g Kennedy-Pendleton heatbath links (%d "
+                        "sweeps from cold, MT seed 42), reference random gauge start (RandSeed "
+                        "351), mixed FP32->FP64 "
                         "OR omega=%g to theta<%g" % ("x".join(map(str, dims)), args.beta,
                                                      args.therm, args.omega, args.eps),
             "lattice": list(dims), "omega": args.omega, "eps": args.eps, "criterion": "theta",

@@ -32,6 +32,7 @@ _LIB_PATH = os.path.join(_HERE, "libgfx.so")
 PREC_DOUBLE, PREC_SINGLE, PREC_MIXED = 0, 1, 2
 LANDAU, COULOMB = 0, 1
 CRIT_MAXDADA, CRIT_THETA, CRIT_THETA_SLICES = 0, 1, 2
+HB_REFERENCE, HB_KENNEDY_PENDLETON = 0, 1
 STATUS = {0: "GFX_OK", 1: "GFX_ERR_BAD_VOLUME", 2: "GFX_ERR_OOM", 3: "GFX_ERR_NOT_CONVERGED",
           4: "GFX_ERR_IO", 5: "GFX_ERR_CUDA", 6: "GFX_ERR_ARG", 7: "GFX_ERR_STATE"}
 
@@ -41,8 +42,15 @@ def library_path():
 
 
 if not os.path.exists(_LIB_PATH):
-    raise ImportError("cudagfx_gb300: %s is missing; build it with "
-                      "`python -m cudagfx_gb300.build` (nvcc, sm_103a)" % _LIB_PATH)
+    # a fresh checkout: compile the library (nvcc, sm_103a); no fallback if that fails
+    try:
+        from . import build as _build
+        _build.build()
+    except Exception as e:  # noqa: BLE001
+        raise ImportError("cudagfx_gb300: %s is missing and could not be built: %s"
+                          % (_LIB_PATH, e)) from e
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError("cudagfx_gb300: %s is missing" % _LIB_PATH)
 
 # RTLD_LOCAL: libgfx defines the reference's globals (LX, VOLUME, FUNC, ...); keep them
 # out of the global namespace so other libraries in the process keep their own.
@@ -89,7 +97,8 @@ class SAParams(_c.Structure):
 
 
 class ThermParams(_c.Structure):
-    _fields_ = [("Nsweep", _c.c_int), ("checkint", _c.c_int), ("beta", _c.c_double)]
+    _fields_ = [("Nsweep", _c.c_int), ("checkint", _c.c_int), ("beta", _c.c_double),
+                ("variant", _c.c_int)]
 
 
 def _sig(name, res, args):
@@ -136,7 +145,7 @@ _sig("gfx_simanneal_range", _I, [_V, _c.POINTER(SAParams), _I, _I])
 _sig("gfx_sa_halfsweep", _I, [_V, _I, _D, _I])
 _sig("gfx_micro_halfsweep", _I, [_V, _I, _I, _I])
 _sig("gfx_thermalize", _I, [_V, _c.POINTER(ThermParams), _dp, _I])
-_sig("gfx_link_heatbath_halfsweep", _I, [_V, _I, _I, _D])
+_sig("gfx_link_heatbath_halfsweep", _I, [_V, _I, _I, _D, _I])
 _sig("gfx_time_sweeps", _I, [_V, _I, _D, _I, _I, _dp])
 _sig("gfx_launch_count", _c.c_ulonglong, [_V])
 _sig("gfx_glibc_rand", None, [_c.c_uint, _I, _i32p])
@@ -398,15 +407,15 @@ class Context:
     def micro_halfsweep(self, parity, gauge=LANDAU, precision=1):
         self._check(lib.gfx_micro_halfsweep(self._h, parity, gauge, precision))
 
-    def thermalize(self, beta, nsweep, checkint=0):
-        p = ThermParams(nsweep, checkint, beta)
-        cap = nsweep // checkint + 1 if checkint > 0 else 0
+    def thermalize(self, beta, nsweep, checkint=0, variant=HB_REFERENCE):
+        p = ThermParams(nsweep, checkint, beta, variant)
+        cap = (nsweep + checkint - 1) // checkint if checkint > 0 else 0
         plaq = np.zeros(max(cap, 1))
         self._check(lib.gfx_thermalize(self._h, _c.byref(p), _ptr(plaq), cap))
         return plaq[:cap]
 
-    def link_heatbath_halfsweep(self, parity, nu, beta):
-        self._check(lib.gfx_link_heatbath_halfsweep(self._h, parity, nu, beta))
+    def link_heatbath_halfsweep(self, parity, nu, beta, variant=HB_REFERENCE):
+        self._check(lib.gfx_link_heatbath_halfsweep(self._h, parity, nu, beta, variant))
 
 
 def sa_temperature(Tmin, Tmax, N, expo, i):

@@ -13,7 +13,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", __import__("platform").machine())
 LIB = os.path.join(HERE, "libgfx.so")
 INCLUDE = os.path.join(ROOT, "include")
 
@@ -70,8 +70,19 @@ def _compile(unit, extra, verbose):
 
 
 def build(verbose=False, force=False, ptxas_info=False):
-    """Compile every unit that is out of date and link libgfx.so; returns its path."""
+    """Compile every unit that is out of date and link libgfx.so; returns its path.
+    Concurrent callers (several ranks on one machine) serialize on a lock file."""
+    import fcntl
     os.makedirs(BUILD, exist_ok=True)
+    with open(os.path.join(BUILD, ".lock"), "w") as lk:
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        try:
+            return _build_locked(verbose, force, ptxas_info)
+        finally:
+            fcntl.flock(lk, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose, force, ptxas_info):
     headers = _headers()
     jobs = []
     for unit, extra in UNITS.items():

@@ -492,9 +492,9 @@ void gfx_or_params_default(gfx_or_params* p) {
   p->omega = 1.68;
   p->criterion = GFX_CRIT_MAXDADA;
   p->gauge = GFX_GAUGE_LANDAU;
-  p->switch_eps = 0.0;
-  p->plateau_ratio = 0.98;
-  p->checkinterval_double = 0;
+  p->switch_eps = 1e-10;
+  p->plateau_ratio = 0.95;
+  p->checkinterval_double = 5;
   p->use_graph = 1;
   p->record_history = 1;
 }
@@ -955,14 +955,15 @@ gfx_status gfx_simanneal(gfx_ctx* ctx, const gfx_sa_params* p, gfx_functional_t*
 // ---------------------------------------------------------------------------
 // thermalization (heatbath_thermalization.cu:557-841)
 // ---------------------------------------------------------------------------
-gfx_status gfx_link_heatbath_halfsweep(gfx_ctx* ctx, int parity, int nu, double beta) {
+gfx_status gfx_link_heatbath_halfsweep(gfx_ctx* ctx, int parity, int nu, double beta,
+                                       int variant) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
   if (!ctx->mt_init) return fail(ctx, GFX_ERR_STATE, "link heatbath needs init_MT");
   if ((long long)kMTCount * ctx->nper_g < 2 * ctx->vol ||
       (long long)kMTCount * ctx->nper_u < 8 * ctx->vol)
     return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
   launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, parity, nu, beta / 3.0, ctx->gauss,
-                       ctx->unif, 128, ctx->stream);
+                       ctx->unif, variant, 128, ctx->stream);
   if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -982,7 +983,7 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
     for (int nu = 0; nu < 4; nu++)
       for (int par = 0; par < 2; par++) {
         launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, par, nu, beta3, ctx->gauss,
-                             ctx->unif, 128, ctx->stream);
+                             ctx->unif, p->variant, 128, ctx->stream);
         enqueue_mt_update(ctx);
       }
     if (i % checkint == 0 && plaq && np < plaq_cap) {

@@ -35,14 +35,46 @@ __device__ __forceinline__ cplx<T> cmk(T re, T im) {
   r.im = im;
   return r;
 }
+// a*b + c with a single rounding: the algebra below is written as explicit FMA
+// chains (a complex multiply-accumulate is four FMAs), which halves the FP32/FP64
+// instruction count compared to separately rounded products and sums.
+template <typename T>
+__device__ __forceinline__ T fm(T a, T b, T c);
+template <>
+__device__ __forceinline__ float fm<float>(float a, float b, float c) {
+  return __fmaf_rn(a, b, c);
+}
+template <>
+__device__ __forceinline__ double fm<double>(double a, double b, double c) {
+  return __fma_rn(a, b, c);
+}
+
 template <typename T>
 __device__ __forceinline__ cplx<T> cmul(cplx<T> a, cplx<T> b) {
-  return cmk<T>(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+  return cmk<T>(fm(a.re, b.re, -a.im * b.im), fm(a.re, b.im, a.im * b.re));
 }
 // a * conj(b)
 template <typename T>
 __device__ __forceinline__ cplx<T> cmulc(cplx<T> a, cplx<T> b) {
-  return cmk<T>(a.re * b.re + a.im * b.im, a.im * b.re - a.re * b.im);
+  return cmk<T>(fm(a.re, b.re, a.im * b.im), fm(a.im, b.re, -a.re * b.im));
+}
+// acc += a * b
+template <typename T>
+__device__ __forceinline__ void cmac(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.re = fm(-a.im, b.im, fm(a.re, b.re, acc.re));
+  acc.im = fm(a.im, b.re, fm(a.re, b.im, acc.im));
+}
+// acc += a * conj(b)
+template <typename T>
+__device__ __forceinline__ void cmacc(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.re = fm(a.im, b.im, fm(a.re, b.re, acc.re));
+  acc.im = fm(-a.re, b.im, fm(a.im, b.re, acc.im));
+}
+// acc += conj(a * b)
+template <typename T>
+__device__ __forceinline__ void cmac_conj(cplx<T>& acc, cplx<T> a, cplx<T> b) {
+  acc.re = fm(-a.im, b.im, fm(a.re, b.re, acc.re));
+  acc.im = fm(-a.im, b.re, fm(-a.re, b.im, acc.im));
 }
 template <typename T>
 __device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) {
@@ -76,12 +108,20 @@ __device__ __forceinline__ void mzero(Mat3<T>& m) {
     for (int j = 0; j < 3; j++) m.e[i][j] = cmk<T>(T(0), T(0));
 }
 
+// conj(p q - r s), one entry of the cross product row
+template <typename T>
+__device__ __forceinline__ cplx<T> cross_conj(cplx<T> p, cplx<T> q, cplx<T> r, cplx<T> s) {
+  const T re = fm(p.re, q.re, fm(-p.im, q.im, fm(-r.re, s.re, r.im * s.im)));
+  const T im = fm(-p.re, q.im, fm(-p.im, q.re, fm(r.re, s.im, r.im * s.re)));
+  return cmk<T>(re, im);
+}
+
 // row 2 = conj(row0 x row1): the 12-real reconstruction (dev_su3.cu:288-305)
 template <typename T>
 __device__ __forceinline__ void row2_from_01(Mat3<T>& g) {
-  g.e[2][0] = cconj(csub(cmul(g.e[0][1], g.e[1][2]), cmul(g.e[0][2], g.e[1][1])));
-  g.e[2][1] = cconj(csub(cmul(g.e[0][2], g.e[1][0]), cmul(g.e[0][0], g.e[1][2])));
-  g.e[2][2] = cconj(csub(cmul(g.e[0][0], g.e[1][1]), cmul(g.e[0][1], g.e[1][0])));
+  g.e[2][0] = cross_conj(g.e[0][1], g.e[1][2], g.e[0][2], g.e[1][1]);
+  g.e[2][1] = cross_conj(g.e[0][2], g.e[1][0], g.e[0][0], g.e[1][2]);
+  g.e[2][2] = cross_conj(g.e[0][0], g.e[1][1], g.e[0][1], g.e[1][0]);
 }
 
 // s += a * b
@@ -90,15 +130,9 @@ __device__ __forceinline__ void addmul(Mat3<T>& s, const Mat3<T>& a, const Mat3<
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) {
-      T re = s.e[i][j].re, im = s.e[i][j].im;
+    for (int j = 0; j < 3; j++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re += a.e[i][k].re * b.e[k][j].re - a.e[i][k].im * b.e[k][j].im;
-        im += a.e[i][k].re * b.e[k][j].im + a.e[i][k].im * b.e[k][j].re;
-      }
-      s.e[i][j] = cmk<T>(re, im);
-    }
+      for (int k = 0; k < 3; k++) cmac(s.e[i][j], a.e[i][k], b.e[k][j]);
 }
 
 // s += a * b^+
@@ -107,74 +141,65 @@ __device__ __forceinline__ void addmul_nd(Mat3<T>& s, const Mat3<T>& a, const Ma
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) {
-      T re = s.e[i][j].re, im = s.e[i][j].im;
+    for (int j = 0; j < 3; j++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re += a.e[i][k].re * b.e[j][k].re + a.e[i][k].im * b.e[j][k].im;
-        im += a.e[i][k].im * b.e[j][k].re - a.e[i][k].re * b.e[j][k].im;
-      }
-      s.e[i][j] = cmk<T>(re, im);
-    }
+      for (int k = 0; k < 3; k++) cmacc(s.e[i][j], a.e[i][k], b.e[j][k]);
 }
 
-// s += (b * a)^+  = a^+ b^+ ; used for the backward star term U^+(x-mu) g^+(x-mu)
+// s += a^+ b^+ = (b a)^+ ; the backward star term U^+(x-mu) g^+(x-mu)
 template <typename T>
 __device__ __forceinline__ void addmul_dd(Mat3<T>& s, const Mat3<T>& a, const Mat3<T>& b) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) {
-      // (a^+ b^+)_ij = sum_k conj(a_ki) conj(b_jk) = conj(sum_k b_jk a_ki)
-      T re = T(0), im = T(0);
+    for (int j = 0; j < 3; j++)
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        re += b.e[j][k].re * a.e[k][i].re - b.e[j][k].im * a.e[k][i].im;
-        im += b.e[j][k].re * a.e[k][i].im + b.e[j][k].im * a.e[k][i].re;
-      }
-      s.e[i][j].re += re;
-      s.e[i][j].im -= im;
-    }
-}
-
-// r = a * b
-template <typename T>
-__device__ __forceinline__ void mul(Mat3<T>& r, const Mat3<T>& a, const Mat3<T>& b) {
-  mzero(r);
-  addmul(r, a, b);
+      for (int k = 0; k < 3; k++) cmac_conj(s.e[i][j], a.e[k][i], b.e[j][k]);
 }
 
 // (a*b)_ij for one entry
 template <typename T>
 __device__ __forceinline__ cplx<T> mul_entry(const Mat3<T>& a, const Mat3<T>& b, int i, int j) {
-  T re = T(0), im = T(0);
+  cplx<T> r = cmul(a.e[i][0], b.e[0][j]);
+  cmac(r, a.e[i][1], b.e[1][j]);
+  cmac(r, a.e[i][2], b.e[2][j]);
+  return r;
+}
+
+// r = a * b
+template <typename T>
+__device__ __forceinline__ void mul(Mat3<T>& r, const Mat3<T>& a, const Mat3<T>& b) {
 #pragma unroll
-  for (int k = 0; k < 3; k++) {
-    re += a.e[i][k].re * b.e[k][j].re - a.e[i][k].im * b.e[k][j].im;
-    im += a.e[i][k].re * b.e[k][j].im + a.e[i][k].im * b.e[k][j].re;
-  }
-  return cmk<T>(re, im);
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) r.e[i][j] = mul_entry(a, b, i, j);
+}
+
+template <typename T>
+__device__ __forceinline__ T row_norm2(const cplx<T>* r) {
+  return fm(r[2].im, r[2].im, fm(r[2].re, r[2].re, fm(r[1].im, r[1].im, fm(r[1].re, r[1].re,
+         fm(r[0].im, r[0].im, r[0].re * r[0].re)))));
 }
 
 // Gram-Schmidt on rows 0,1 (dev_su3.cu:1569-1615); row 2 only when asked
 template <typename T, bool ROW2>
 __device__ __forceinline__ void normalize(Mat3<T>& u) {
-  T len = u.e[0][0].re * u.e[0][0].re + u.e[0][0].im * u.e[0][0].im + u.e[0][1].re * u.e[0][1].re +
-          u.e[0][1].im * u.e[0][1].im + u.e[0][2].re * u.e[0][2].re + u.e[0][2].im * u.e[0][2].im;
-  len = rsqrt_t<T>(len);
+  T len = rsqrt_t<T>(row_norm2<T>(u.e[0]));
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     u.e[0][i].re *= len;
     u.e[0][i].im *= len;
   }
-  cplx<T> proj = cmk<T>(T(0), T(0));
+  cplx<T> proj = cmulc(u.e[1][0], u.e[0][0]);
+  cmacc(proj, u.e[1][1], u.e[0][1]);
+  cmacc(proj, u.e[1][2], u.e[0][2]);
 #pragma unroll
-  for (int i = 0; i < 3; i++) proj = cadd(proj, cmulc(u.e[1][i], u.e[0][i]));
-#pragma unroll
-  for (int i = 0; i < 3; i++) u.e[1][i] = csub(u.e[1][i], cmul(proj, u.e[0][i]));
-  len = u.e[1][0].re * u.e[1][0].re + u.e[1][0].im * u.e[1][0].im + u.e[1][1].re * u.e[1][1].re +
-        u.e[1][1].im * u.e[1][1].im + u.e[1][2].re * u.e[1][2].re + u.e[1][2].im * u.e[1][2].im;
-  len = rsqrt_t<T>(len);
+  for (int i = 0; i < 3; i++) {
+    const cplx<T> b = u.e[1][i], a = u.e[0][i];
+    u.e[1][i].re = fm(proj.im, a.im, fm(-proj.re, a.re, b.re));
+    u.e[1][i].im = fm(-proj.im, a.re, fm(-proj.re, a.im, b.im));
+  }
+  len = rsqrt_t<T>(row_norm2<T>(u.e[1]));
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     u.e[1][i].re *= len;
@@ -207,16 +232,19 @@ __device__ __forceinline__ Su2<T> su2_extract(const Mat3<T>& g, const Mat3<T>& s
   return w;
 }
 
-// rows a,b of g <- alpha acting from the left (overrelax.cu:244-265)
+// rows a,b of g <- alpha acting from the left (overrelax.cu:244-265):
+//   row_a' = (a0 + i a3) row_a + (a2 + i a1) row_b
+//   row_b' = (-a2 + i a1) row_a + (a0 - i a3) row_b
 template <typename T>
 __device__ __forceinline__ void su2_rotate(Mat3<T>& g, int a, int b, const Su2<T>& al) {
+  const T a0 = al.v[0], a1 = al.v[1], a2 = al.v[2], a3 = al.v[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) {
-    cplx<T> ga = g.e[a][c], gb = g.e[b][c];
-    cplx<T> na = cadd(cmul(cmk<T>(al.v[0], al.v[3]), ga), cmul(cmk<T>(al.v[2], al.v[1]), gb));
-    cplx<T> nb = cadd(cmul(cmk<T>(-al.v[2], al.v[1]), ga), cmul(cmk<T>(al.v[0], -al.v[3]), gb));
-    g.e[a][c] = na;
-    g.e[b][c] = nb;
+    const cplx<T> ga = g.e[a][c], gb = g.e[b][c];
+    g.e[a][c].re = fm(-a1, gb.im, fm(a2, gb.re, fm(-a3, ga.im, a0 * ga.re)));
+    g.e[a][c].im = fm(a1, gb.re, fm(a2, gb.im, fm(a3, ga.re, a0 * ga.im)));
+    g.e[b][c].re = fm(a3, gb.im, fm(a0, gb.re, fm(-a1, ga.im, -a2 * ga.re)));
+    g.e[b][c].im = fm(-a3, gb.re, fm(a0, gb.im, fm(a1, ga.re, -a2 * ga.im)));
   }
 }
 
@@ -278,29 +306,22 @@ __device__ __forceinline__ void overrelax_rows01(Mat3<T>& gout, const Mat3<T>& g
   const T c2 = omega * (omega - T(1)) * T(0.5);
 #pragma unroll
   for (int r = 0; r < 2; r++) {
-    // R_rk = (D gold^+)_rk
+    // c2 * R_rk with R = D gold^+
     cplx<T> R[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      T re = T(0), im = T(0);
-#pragma unroll
-      for (int l = 0; l < 3; l++) {
-        re += D.e[r][l].re * gold.e[k][l].re + D.e[r][l].im * gold.e[k][l].im;
-        im += D.e[r][l].im * gold.e[k][l].re - D.e[r][l].re * gold.e[k][l].im;
-      }
-      R[k] = cmk<T>(re, im);
+      cplx<T> x = cmulc(D.e[r][0], gold.e[k][0]);
+      cmacc(x, D.e[r][1], gold.e[k][1]);
+      cmacc(x, D.e[r][2], gold.e[k][2]);
+      R[k] = cmk<T>(c2 * x.re, c2 * x.im);
     }
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      T re = gold.e[r][j].re + omega * D.e[r][j].re;
-      T im = gold.e[r][j].im + omega * D.e[r][j].im;
-      T rr = T(0), ri = T(0);
+      cplx<T> o = cmk<T>(fm(omega, D.e[r][j].re, gold.e[r][j].re),
+                         fm(omega, D.e[r][j].im, gold.e[r][j].im));
 #pragma unroll
-      for (int k = 0; k < 3; k++) {
-        rr += R[k].re * D.e[k][j].re - R[k].im * D.e[k][j].im;
-        ri += R[k].re * D.e[k][j].im + R[k].im * D.e[k][j].re;
-      }
-      gout.e[r][j] = cmk<T>(re + c2 * rr, im + c2 * ri);
+      for (int k = 0; k < 3; k++) cmac(o, R[k], D.e[k][j]);
+      gout.e[r][j] = o;
     }
   }
   normalize<T, false>(gout);

@@ -74,6 +74,45 @@ __device__ __forceinline__ void cm_heatbath(Mat3<T>& g, const Mat3<T>& star, dou
   }
 }
 
+// Kennedy-Pendleton SU(2) heatbath for the Wilson action: the subgroup weight is
+// exp(beta * alpha.w) with beta = beta_lattice/3, so a0 has density
+// sqrt(1-a0^2) exp(beta |w| a0).  One trial: 2 lambda^2 = (E + g^2/2) / (beta |w|)
+// with E exponential and g standard normal, a0 = 1 - 2 lambda^2, accepted when
+// u^2 <= 1 - lambda^2; a rejected trial leaves the subgroup unchanged (the chain
+// still has the Wilson-action distribution as its fixed point).
+template <typename T>
+__device__ __forceinline__ Su2<T> heatbath_su2_kp(const Su2<T>& wt, double beta, float gauss,
+                                                  float4 u) {
+  const double w[4] = {(double)wt.v[0], (double)wt.v[1], (double)wt.v[2], (double)wt.v[3]};
+  const double k = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  Su2<T> al;
+  al.v[0] = T(1);
+  al.v[1] = al.v[2] = al.v[3] = T(0);
+  if (!(k > 0.0)) return al;
+  const double rk = 1.0 / k;
+  const double E = -log(1.0 - (double)u.x);
+  const double y = (E + 0.5 * (double)gauss * (double)gauss) / (beta * k);
+  if (!((double)u.y * (double)u.y <= 1.0 - 0.5 * y)) return al;
+  double v[4];
+#pragma unroll
+  for (int i = 0; i < 4; i++) v[i] = w[i] * rk;
+  double a[4];
+  a[0] = 1.0 - y;
+  const double norm = sqrt(fmax(0.0, 1.0 - a[0] * a[0]));
+  const double cos_theta = 2.0 * (double)u.z - 1.0;
+  const double sin_theta = sqrt(fmax(0.0, 1.0 - cos_theta * cos_theta));
+  double sphi, cphi;
+  sincospi(2.0 * (double)u.w, &sphi, &cphi);
+  a[1] = norm * sin_theta * cphi;
+  a[2] = norm * sin_theta * sphi;
+  a[3] = norm * cos_theta;
+  al.v[0] = (T)(a[0] * v[0] - a[1] * v[1] - a[2] * v[2] - a[3] * v[3]);
+  al.v[1] = (T)(a[0] * v[1] + a[1] * v[0] - a[2] * v[3] + a[3] * v[2]);
+  al.v[2] = (T)(a[0] * v[2] + a[2] * v[0] - a[3] * v[1] + a[1] * v[3]);
+  al.v[3] = (T)(a[0] * v[3] + a[3] * v[0] - a[1] * v[2] + a[2] * v[1]);
+  return al;
+}
+
 // star for the gauge-transformation update (same as the OR kernel)
 template <typename T, int NRU, int NDIR>
 __device__ __forceinline__ void g_star(const Lattice& L, const Site& c, int parity,
@@ -192,7 +231,10 @@ __device__ __forceinline__ void ld_link(const Lattice& L, const double2* __restr
   Field<double, NR>::load(U + (size_t)(p * 4 + mu) * NC * L.vh, (size_t)L.vh, i, m);
 }
 
-template <int NR>
+// VARIANT 0: the reference's update (one random set per link, all subgroups);
+// VARIANT 1: Kennedy-Pendleton, subgroup s draws slot 4*i + ((nu + s) & 3) of the
+// fields, so the three subgroups use independent numbers.
+template <int NR, int VARIANT>
 __global__ void __launch_bounds__(128) link_heatbath_kernel(Lattice L, double2* U, int parity,
                                                              int nu, double beta3,
                                                              const float* gauss,
@@ -229,21 +271,37 @@ __global__ void __launch_bounds__(128) link_heatbath_kernel(Lattice L, double2* 
   double2* blk = U + (size_t)(parity * 4 + nu) * NC * L.vh;
   Mat3<double> link;
   Field<double, NR>::load(blk, (size_t)L.vh, i, link);
-  const int r = 4 * i + nu;
-  cm_heatbath(link, staple, beta3, __ldg(gauss + r), __ldg(unif4 + r));
+  if (VARIANT == 0) {
+    const int r = 4 * i + nu;
+    cm_heatbath(link, staple, beta3, __ldg(gauss + r), __ldg(unif4 + r));
+  } else {
+#pragma unroll
+    for (int sg = 0; sg < 3; sg++) {
+      const int r = 4 * i + ((nu + sg) & 3);
+      const int a = sub_a(sg), b = sub_b(sg);
+      Su2<double> w = su2_extract(link, staple, a, b);
+      su2_rotate(link, a, b, heatbath_su2_kp(w, beta3, __ldg(gauss + r), __ldg(unif4 + r)));
+    }
+  }
   normalize<double, true>(link);
   Field<double, NR>::store(blk, (size_t)L.vh, i, link);
 }
 
 void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu, double beta3,
-                          const float* gauss, const float* unif, int block, cudaStream_t s) {
+                          const float* gauss, const float* unif, int variant, int block,
+                          cudaStream_t s) {
   dim3 grid((L.vh + block - 1) / block);
-  if (link_nr == 18)
-    link_heatbath_kernel<18><<<grid, block, 0, s>>>(L, (double2*)U, parity, nu, beta3, gauss,
-                                                     (const float4*)unif);
-  else
-    link_heatbath_kernel<12><<<grid, block, 0, s>>>(L, (double2*)U, parity, nu, beta3, gauss,
-                                                     (const float4*)unif);
+#define LHB(NR, VAR)                                                                \
+  link_heatbath_kernel<NR, VAR><<<grid, block, 0, s>>>(L, (double2*)U, parity, nu, beta3, \
+                                                       gauss, (const float4*)unif)
+  if (link_nr == 18) {
+    if (variant) LHB(18, 1);
+    else LHB(18, 0);
+  } else {
+    if (variant) LHB(12, 1);
+    else LHB(12, 0);
+  }
+#undef LHB
 }
 
 }  // namespace gfx

@@ -74,8 +74,8 @@ void launch_sa_heatbath(int prec, int link_nr, const Lattice& L, const void* U, 
 void launch_micro(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
                   int parity, int block, cudaStream_t s);
 void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu,
-                          double beta3, const float* gauss, const float* unif, int block,
-                          cudaStream_t s);
+                          double beta3, const float* gauss, const float* unif, int variant,
+                          int block, cudaStream_t s);
 
 // ----- Mersenne Twister bank (gfx_mt.cu) -----
 struct MTBank {

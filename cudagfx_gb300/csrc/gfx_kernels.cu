@@ -319,10 +319,11 @@ __global__ void final_reduce_kernel(const double* slice_sums, int lt, double vol
   S.last_theta_slice_max = r.theta_slice_max;
   int done = 0;
   if (S.phase == 0) {
-    // single-precision phase: hand over to the double-precision phase when the
-    // monitored value reaches the switch threshold or stops decreasing
-    if (value < S.switch_eps || value < S.eps ||
-        (S.prev > 0.0 && value > S.plateau_ratio * S.prev))
+    // single-precision phase: hand over to the double-precision phase when the target
+    // is reached (the FP64 phase verifies it), or when, below switch_eps, the value
+    // stops decreasing -- the FP32 rounding floor, which a few FP64 sweeps remove
+    if (value < S.eps ||
+        (value < S.switch_eps && S.prev > 0.0 && value > S.plateau_ratio * S.prev))
       done = 2;
   } else if (value < S.eps) {
     done = 1;

@@ -244,6 +244,7 @@ void thermalize_gauge(void) {
   tp.Nsweep = 1;
   tp.checkint = 0;
   tp.beta = thermparam.beta;
+  tp.variant = GFX_HB_REFERENCE;
   const int ck = thermparam.checkint > 0 ? thermparam.checkint : 1;
   for (int i = 0; i < thermparam.Nsweep; i++) {
     if (gfx_thermalize(g_ctx, &tp, nullptr, 0) != GFX_OK) {

@@ -67,8 +67,8 @@ typedef struct {
   double omega;           /* overrelaxation parameter (reference: 1.68, overrelax.cu:416) */
   int criterion;          /* gfx_criterion */
   int gauge;              /* gfx_gauge */
-  double switch_eps;      /* mixed: leave the FP32 phase when its value drops below this */
-  double plateau_ratio;   /* mixed: ... or when value_new > plateau_ratio * value_old */
+  double switch_eps;      /* mixed: below this the FP32 phase ends when the value stalls */
+  double plateau_ratio;   /* mixed: stalled = value_new > plateau_ratio * value_old */
   int checkinterval_double; /* sweeps between checks in the FP64 phase (0: checkinterval) */
   int use_graph;          /* 1: device-side loop in a CUDA graph (conditional while node) */
   int record_history;     /* keep every check (gfx_or_history) */
@@ -103,7 +103,15 @@ typedef struct {
   int Nsweep;
   int checkint;
   double beta;
+  int variant; /* GFX_HB_REFERENCE or GFX_HB_KENNEDY_PENDLETON */
 } gfx_therm_params;
+
+/* Link-heatbath variants.  REFERENCE reproduces the reference's update
+ * (heatbath_thermalization.cu:493-550 with simulated_annealing.cu:5-142: one trial
+ * with k = |w|^2, the same random numbers for all three subgroups, alpha = w on
+ * rejection).  KENNEDY_PENDLETON samples the Wilson-action distribution at beta
+ * (k = |w|, independent numbers per subgroup, no update on rejection). */
+enum { GFX_HB_REFERENCE = 0, GFX_HB_KENNEDY_PENDLETON = 1 };
 
 /* ---- library / context ---- */
 int gfx_abi_version(void);
@@ -189,7 +197,8 @@ gfx_status gfx_micro_halfsweep(gfx_ctx *ctx, int parity, int gauge, int precisio
  * beta/3 per set_beta; plaquette every checkint sweeps into plaq (if non-NULL, capacity
  * Nsweep/checkint + 1).  The result stays on the device (gfx_get_links). */
 gfx_status gfx_thermalize(gfx_ctx *ctx, const gfx_therm_params *p, double *plaq, int plaq_cap);
-gfx_status gfx_link_heatbath_halfsweep(gfx_ctx *ctx, int parity, int nu, double beta);
+gfx_status gfx_link_heatbath_halfsweep(gfx_ctx *ctx, int parity, int nu, double beta,
+                                       int variant);
 
 /* ---- host-side helpers ---- */
 /* page-locked host memory for the field copies (cudaMallocHost); NULL on failure */

