@@ -584,7 +584,9 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   LoopState& H = *ctx->loop_host;
   std::memset(&H, 0, sizeof(H));
   H.iter = 0;
-  H.ck = prec == 0 ? p.checkinterval : p.checkinterval_double;
+  // checkinterval_double applies to the FP64 polish after a mixed-precision handover;
+  // a single-precision-mode run checks every checkinterval sweeps (overrelax.cu:775)
+  H.ck = p.checkinterval;
   H.maxit = p.maxit;
   H.criterion = p.criterion;
   H.phase = handover ? 0 : 1;
