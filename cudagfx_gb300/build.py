@@ -27,6 +27,7 @@ UNITS = {
     "gfx_heatbath.cu": [],
     "gfx_mt.cu": ["-prec-sqrt=false", "-prec-div=false", "-ftz=false"],
     "gfx_api.cu": [],
+    "gfx_noalloc.cu": [],
     "gfx_host.cpp": [],
     "gfx_legacy.cpp": [],
 }

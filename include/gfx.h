@@ -159,6 +159,22 @@ gfx_status gfx_polyakov(gfx_ctx *ctx, double *re_im);
  * (dev_apply_trafo overrelax.cu:273-331 / g_trafo observables.c:17-47) */
 gfx_status gfx_apply_trafo(gfx_ctx *ctx);
 
+/* No counterpart in the reference.  The functional and theta (gfx_functional_t layout,
+ * written to result_device: 5 doubles in device memory) of fields the caller already
+ * holds in device memory, for callers that cannot allocate device memory while they
+ * run -- a framework that owns every device byte through its own pool, or a service
+ * with a device footprint fixed at start-up.  Nothing is allocated: the reduction
+ * scratch is a fixed file-scope device array (about 0.8 MB per device, held until the
+ * process exits) with room for lt <= 1024 time slices; larger lt returns GFX_ERR_ARG.
+ * links_device: FP64 links in the library's even/odd layout (link_reals 12 or 18
+ * doubles per link, as a context stores them); trafo_device: FP64 12-real g in the
+ * same layout; stream: a cudaStream_t or NULL.  The first call on a device looks up
+ * the scratch array's address (make it before any stream capture).  All calls on a
+ * device share the array; calls that overlap on the GPU race.  Asynchronous on stream. */
+gfx_status gfx_functional_noalloc(const void *links_device, const void *trafo_device, int lx,
+                                  int ly, int lz, int lt, int link_reals, int gauge,
+                                  double *result_device, void *stream);
+
 /* device time (CUDA events on the context's stream) of nsweeps plain OR sweeps */
 gfx_status gfx_time_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision,
                            double *ms);
