@@ -39,9 +39,9 @@ UNIT = "site-updates/s"
 BYTES_PER_UPDATE_FP32 = 132 * 4
 BYTES_PER_UPDATE_FP64 = 132 * 8
 FLOP_PER_UPDATE = 4766  # the reference's count (overrelax.cu:897)
-# DRAM bytes per FP32 half-sweep launch at 32^4, read+write, from the ncu capture
-# summarised in profiles/or_halfsweep_fp32_32x4.md (None until captured)
-NCU_TRAFFIC_FP32 = None
+# DRAM bytes per FP32 half-sweep launch at 32^4 (dram__bytes_read.sum +
+# dram__bytes_write.sum), from the ncu capture in profiles/or_halfsweep_fp32_32x4.md
+NCU_TRAFFIC_FP32 = {(32, 32, 32, 32): 254.05e6 + 15.68e6}
 
 
 def parse():
@@ -59,8 +59,39 @@ def parse():
     ap.add_argument("--switch-eps", type=float, default=1e-10)
     ap.add_argument("--checkinterval-double", type=int, default=5)
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="host-driven check loop instead of the CUDA-graph while loop (same "
+                         "kernels; profilers list each launch)")
     ap.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample sweeps (0: auto)")
+    ap.add_argument("--kernels", action="store_true",
+                    help="no timing: a few launches of each hot kernel on the lattice, for "
+                         "ncu captures")
     return ap.parse_args()
+
+
+def run_kernels(args, dims):
+    """A short fixed workload for profiler captures: 3 FP32 OR sweeps, an FP32 and an
+    FP64 functional, 1 FP64 OR sweep, one SA step and one link-heatbath sweep."""
+    import cudagfx_gb300 as gfx
+    V = int(np.prod(dims))
+    ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    ctx.set_links(gfx.random_init_haar(11, 4 * V))
+    ctx.set_trafo(gfx.random_init_reference(351, V))
+    ctx.or_sweeps(3, omega=args.omega, precision=0)
+    ctx.functional(precision=0)
+    ctx.functional(precision=1)
+    ctx.or_sweeps(1, omega=args.omega, precision=1)
+    dat = mt_params_path()
+    if dat:
+        ctx.mt_load_file(dat)
+    else:
+        ctx.mt_load_params(synthetic_mt_params())
+    ctx.mt_seed(42)
+    ctx.mt_init(2 * V, 8 * V)
+    ctx.simanneal(0.5, 0.5, 1)
+    ctx.thermalize(args.beta, 1, variant=gfx.HB_KENNEDY_PENDLETON)
+    ctx.close()
+    print("kernels ok")
 
 
 # ---------------------------------------------------------------------------
@@ -263,10 +294,11 @@ def run_gfx(args, dims):
     plaq = ctx.plaquette()
     links = ctx.get_links()
     g0 = gfx.random_init_reference(351 + rank, V)
-    params = ctx.or_params(maxit=200000, eps=args.eps, checkinterval=args.checkinterval,
+    params = ctx.or_params(maxit=20000, eps=args.eps, checkinterval=args.checkinterval,
                            omega=args.omega, criterion=gfx.CRIT_THETA,
                            switch_eps=args.switch_eps,
-                           checkinterval_double=args.checkinterval_double)
+                           checkinterval_double=args.checkinterval_double,
+                           use_graph=0 if args.no_graph else 1)
 
     def solve(c):
         c.set_trafo(g0)
@@ -333,7 +365,7 @@ def run_gfx(args, dims):
     roof = {"bound": "hbm", "kernel": "or_halfsweep_kernel<float,12,4>",
             "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
             "peak_source": peak_kind,
-            "traffic": NCU_TRAFFIC_FP32, "ms_per_launch": ms32,
+            "traffic": NCU_TRAFFIC_FP32.get(tuple(dims)), "ms_per_launch": ms32,
             "bytes_per_launch": bytes32,
             "time_share_in_solve": t32_share / max(r_last.ms, 1e-9)}
     if ms64:
@@ -386,7 +418,9 @@ def run_gfx(args, dims):
 def main():
     args = parse()
     dims = tuple(int(x) for x in args.dims.split(","))
-    if args.impl == "reference":
+    if args.kernels:
+        run_kernels(args, dims)
+    elif args.impl == "reference":
         run_reference(args, dims)
     else:
         run_gfx(args, dims)
