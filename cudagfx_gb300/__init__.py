@@ -301,6 +301,9 @@ class Context:
     def unit_trafo(self):
         self._check(lib.gfx_unit_trafo(self._h))
 
+    def random_trafo_haar(self, seed):
+        self._check(lib.gfx_random_trafo_haar(self._h, seed))
+
     # ---- gauge fixing
     @staticmethod
     def or_params(**kw):
@@ -416,6 +419,94 @@ class Context:
 
     def link_heatbath_halfsweep(self, parity, nu, beta, variant=HB_REFERENCE):
         self._check(lib.gfx_link_heatbath_halfsweep(self._h, parity, nu, beta, variant))
+
+
+class CopyResult(_c.Structure):
+    _fields_ = [("conf", _c.c_int), ("copy", _c.c_int), ("converged", _c.c_int),
+                ("iterations", _c.c_int), ("sweeps", _c.c_int), ("sweeps_single", _c.c_int),
+                ("sweeps_double", _c.c_int), ("F", _c.c_double), ("dAdA", _c.c_double),
+                ("maxdAdA", _c.c_double), ("theta", _c.c_double),
+                ("theta_slice_max", _c.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_sig("gfx_batch_create", _I, [_c.POINTER(_V), _I, _c.POINTER(_I), _c.POINTER(_I), _I, _I, _V])
+_sig("gfx_batch_destroy", _I, [_V])
+_sig("gfx_batch_last_error", _c.c_char_p, [_V])
+_sig("gfx_batch_copies", _I, [_V])
+_sig("gfx_batch_set_links", _I, [_V, _I, _dp])
+_sig("gfx_batch_set_trafo", _I, [_V, _I, _I, _dp])
+_sig("gfx_batch_get_trafo", _I, [_V, _I, _I, _dp])
+_sig("gfx_batch_random_haar", _I, [_V, _c.c_uint64])
+_sig("gfx_batch_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(CopyResult), _dp])
+_sig("gfx_batch_best", _I, [_V, _c.POINTER(CopyResult), _I, _c.POINTER(_I), _dp])
+_sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])
+
+
+class Batch:
+    """Gauge copies of several configurations fixed together (gfx_batch_*)."""
+
+    def __init__(self, dims_list, ncopies, precision=PREC_MIXED, copies_per_item=0, stream=None):
+        n = len(dims_list)
+        d = (_I * (4 * n))(*[x for dims in dims_list for x in dims])
+        c = (_I * n)(*ncopies)
+        h = _V()
+        s = lib.gfx_batch_create(_c.byref(h), n, d, c, precision, copies_per_item,
+                                 _V(stream) if stream else None)
+        if s != 0:
+            raise GfxError(s, lib.gfx_batch_last_error(None).decode())
+        self._h = h
+        self.dims = [tuple(x) for x in dims_list]
+        self.ncopies = list(ncopies)
+        self.total = lib.gfx_batch_copies(h)
+
+    def _check(self, s, ok=(0,)):
+        if s not in ok:
+            raise GfxError(s, lib.gfx_batch_last_error(self._h).decode())
+        return s
+
+    def close(self):
+        if self._h:
+            lib.gfx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_links(self, conf, u):
+        v = int(np.prod(self.dims[conf]))
+        self._check(lib.gfx_batch_set_links(self._h, conf, _ptr(_f64(u, 4 * v))))
+
+    def set_trafo(self, conf, copy, g):
+        v = int(np.prod(self.dims[conf]))
+        self._check(lib.gfx_batch_set_trafo(self._h, conf, copy, _ptr(_f64(g, v))))
+
+    def get_trafo(self, conf, copy):
+        out = np.empty((int(np.prod(self.dims[conf])), 3, 3, 2))
+        self._check(lib.gfx_batch_get_trafo(self._h, conf, copy, _ptr(out)))
+        return out
+
+    def random_haar(self, seed):
+        self._check(lib.gfx_batch_random_haar(self._h, seed))
+
+    def overrelax(self, params=None, **kw):
+        p = params if params is not None else Context.or_params(**kw)
+        res = (CopyResult * self.total)()
+        ms = np.zeros(1)
+        self._check(lib.gfx_batch_overrelax(self._h, _c.byref(p), res, _ptr(ms)), ok=(0, 3))
+        self.last_results = res
+        return [r.as_dict() for r in res], float(ms[0])
+
+    def best(self, conf):
+        k, f = _I(), np.zeros(1)
+        self._check(lib.gfx_batch_best(self._h, self.last_results, conf, _c.byref(k), _ptr(f)),
+                    ok=(0, 3))
+        return k.value, float(f[0])
 
 
 def sa_temperature(Tmin, Tmax, N, expo, i):

@@ -28,6 +28,7 @@ UNITS = {
     "gfx_mt.cu": ["-prec-sqrt=false", "-prec-div=false", "-ftz=false"],
     "gfx_api.cu": [],
     "gfx_noalloc.cu": [],
+    "gfx_batch.cu": [],
     "gfx_host.cpp": [],
     "gfx_legacy.cpp": [],
 }

@@ -1,0 +1,757 @@
+// gfx_batch.cu -- many gauge copies of several configurations, fixed together.
+//
+// A batch holds nconf configurations (each with its own lattice extents and links) and
+// ncopies[c] gauge transformations per configuration (Gribov copies).  Every half-sweep
+// of every active copy of every configuration is one kernel launch: a work item is
+// (configuration, block of 128 sites, group of K copies).  The item's threads stage
+// the 8 links of their site (4 forward, 4 backward) once in shared memory and update
+// the K copies with them, so each link read from HBM serves K copy updates.  The
+// checks, their per-copy reductions and the per-copy convergence bookkeeping run on
+// the device; the whole loop is one CUDA graph with a conditional while node, as for a
+// single lattice.  Per copy, the arithmetic and the reduction order are those of the
+// single-lattice kernels (gfx_common.cuh), so a copy's trajectory, iteration count and
+// final functional equal those of the same start fixed alone.
+#include <algorithm>
+#include <array>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gfx.h"
+#include "gfx_common.cuh"
+#include "gfx_internal.h"
+
+namespace gfx {
+
+constexpr int kBatchBlock = 128;
+constexpr int kMaxConf = 8;
+
+struct BConf {
+  Lattice L;
+  const void* U32;   // FP32 12-real links
+  const void* U64;   // FP64 12-real links
+  void* G32;         // copy 0's g (FP32), copy k at + k * gstride32 vectors
+  void* G64;         // copy 0's g (FP64), copy k at + k * gstride64 vectors
+  size_t gstride32, gstride64;
+  int ncopies;
+  int copy_base;     // index of copy 0 among all copies of the batch
+  int item_base;     // first sweep work item
+  int nblk;          // site blocks per parity
+  int ngroups;       // copy groups of K
+  int mitem_base;    // first measurement item
+  int nbx;           // measurement blocks per time slice
+  size_t part_base;  // first partial triple of copy 0 (copy k: + k * 2 * lt * nbx)
+  int slice_base;    // first slice triple of copy 0 (copy k: + k * lt)
+  int sitem_base;    // first slice-reduce item
+};
+
+struct BDesc {
+  BConf c[kMaxConf];
+  int nconf;
+  int ncopies;  // all configurations
+  int K;        // copies per sweep item
+  LoopState* states;
+  double* partials;
+  double* slice_sums;
+  Reduced* reduced;
+};
+
+__device__ __forceinline__ int conf_of(const BDesc& d, int item, int BConf::*base) {
+  int ci = 0;
+  while (ci + 1 < d.nconf && item >= d.c[ci + 1].*base) ci++;
+  return ci;
+}
+
+template <typename T>
+__device__ __forceinline__ void smem_load12(const typename VecOf<T>::type* sl, int link, int tid,
+                                            Mat3<T>& m);
+template <>
+__device__ __forceinline__ void smem_load12<float>(const float4* sl, int link, int tid,
+                                                   Mat3<float>& m) {
+  const float4 a = sl[(link * 3 + 0) * kBatchBlock + tid];
+  const float4 b = sl[(link * 3 + 1) * kBatchBlock + tid];
+  const float4 c = sl[(link * 3 + 2) * kBatchBlock + tid];
+  m.e[0][0] = cmk(a.x, a.y);
+  m.e[0][1] = cmk(a.z, a.w);
+  m.e[0][2] = cmk(b.x, b.y);
+  m.e[1][0] = cmk(b.z, b.w);
+  m.e[1][1] = cmk(c.x, c.y);
+  m.e[1][2] = cmk(c.z, c.w);
+  row2_from_01(m);
+}
+template <>
+__device__ __forceinline__ void smem_load12<double>(const double2* sl, int link, int tid,
+                                                    Mat3<double>& m) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const double2 v = sl[(link * 6 + k) * kBatchBlock + tid];
+    m.e[k / 3][k % 3] = cmk(v.x, v.y);
+  }
+  row2_from_01(m);
+}
+
+// One half-sweep of parity `parity` for all active copies (or_halfsweep_kernel per copy)
+template <typename T, int NDIR>
+__global__ void __launch_bounds__(kBatchBlock) or_batch_kernel(BDesc d, int parity, T omega) {
+  typedef typename VecOf<T>::type V;
+  constexpr int NC = Field<T, 12>::NCHUNK;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* sl = reinterpret_cast<V*>(smem_raw);  // [8 links][NC][block]
+  const int ci = conf_of(d, blockIdx.x, &BConf::item_base);
+  const BConf& C = d.c[ci];
+  const int local = blockIdx.x - C.item_base;
+  const int grp = local / C.nblk, blk = local - grp * C.nblk;
+  const int tid = threadIdx.x;
+  const int i = blk * kBatchBlock + tid;
+  if (i >= C.L.vh) return;
+  const size_t vh = (size_t)C.L.vh;
+  const int q = 1 - parity;
+  const Site s = site_of(C.L, i, parity);
+  const V* U = (const V*)(sizeof(T) == 4 ? C.U32 : C.U64);
+  // every thread stages its own site's links; no other thread reads them
+#pragma unroll
+  for (int mu = 0; mu < NDIR; mu++) {
+    const V* Uf = U + (size_t)(parity * 4 + mu) * NC * vh;
+    const V* Ub = U + (size_t)(q * 4 + mu) * NC * vh;
+    const int jb = nb_bwd(C.L, s, mu);
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+      sl[(mu * NC + c) * kBatchBlock + tid] = __ldg(Uf + c * vh + i);
+      sl[((4 + mu) * NC + c) * kBatchBlock + tid] = __ldg(Ub + c * vh + jb);
+    }
+  }
+  V* G0 = (V*)(sizeof(T) == 4 ? C.G32 : C.G64);
+  const size_t gstride = sizeof(T) == 4 ? C.gstride32 : C.gstride64;
+#pragma unroll 1
+  for (int k = 0; k < d.K; k++) {
+    const int copy = grp * d.K + k;
+    if (copy >= C.ncopies) break;
+    if (d.states[C.copy_base + copy].done != 0) continue;
+    V* G = G0 + (size_t)copy * gstride;
+    const V* Gq = G + (size_t)q * NC * vh;
+    Mat3<T> star;
+    mzero(star);
+#pragma unroll
+    for (int mu = 0; mu < NDIR; mu++) {
+      Mat3<T> a, b;
+      smem_load12<T>(sl, mu, tid, a);
+      Field<T, 12>::load(Gq, vh, nb_fwd(C.L, s, mu), b);
+      addmul_nd(star, a, b);
+      const int jb = nb_bwd(C.L, s, mu);
+      smem_load12<T>(sl, 4 + mu, tid, a);
+      Field<T, 12>::load(Gq, vh, jb, b);
+      addmul_dd(star, a, b);
+    }
+    V* Gp = G + (size_t)parity * NC * vh;
+    Mat3<T> gold, g, gn;
+    Field<T, 12>::load(Gp, vh, i, gold);
+    g = gold;
+    cm_relax(g, star);
+    normalize<T, true>(g);
+    overrelax_rows01(gn, gold, g, omega);
+    Field<T, 12>::store(Gp, vh, i, gn);
+  }
+}
+
+// Per-copy functional partials (measure_kernel per copy, same block grouping)
+template <typename TC, typename TSG, int NDIR>
+__global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
+  const int ci = conf_of(d, blockIdx.x, &BConf::mitem_base);
+  const BConf& C = d.c[ci];
+  int local = blockIdx.x - C.mitem_base;
+  const int per_copy = 2 * C.L.lt * C.nbx;
+  const int copy = local / per_copy;
+  local -= copy * per_copy;
+  const int parity = local / (C.L.lt * C.nbx);
+  local -= parity * C.L.lt * C.nbx;
+  const int t = local / C.nbx, bx = local - t * C.nbx;
+  if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  typedef typename VecOf<TC>::type VU;
+  typedef typename VecOf<TSG>::type VG;
+  const VU* U = (const VU*)(sizeof(TC) == 4 ? C.U32 : C.U64);
+  const VG* G = (const VG*)(sizeof(TSG) == 4 ? C.G32 : C.G64) +
+                (size_t)copy * (sizeof(TSG) == 4 ? C.gstride32 : C.gstride64);
+  const int k = bx * blockDim.x + threadIdx.x;
+  double f = 0.0, dd = 0.0;
+  if (k < C.L.st) {
+    const int i = t * C.L.st + k;
+    const Site c = site_of(C.L, i, parity);
+    Mat3<TC> star, g;
+    compute_star<TC, TC, 12, TSG, 12, NDIR>(C.L, c, parity, U, G, star);
+    constexpr int NCG = Field<TSG, 12>::NCHUNK;
+    Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * C.L.vh, (size_t)C.L.vh, i, g);
+    site_functional(g, star, f, dd);
+  }
+  double* out = d.partials +
+                3 * (C.part_base + (size_t)copy * per_copy + (size_t)(parity * C.L.lt + t) * C.nbx + bx);
+  block_reduce3(f, dd, dd, out);
+}
+
+// per (copy, slice) sums, as slice_reduce_kernel
+__global__ void slice_batch_kernel(BDesc d) {
+  const int ci = conf_of(d, blockIdx.x, &BConf::sitem_base);
+  const BConf& C = d.c[ci];
+  const int local = blockIdx.x - C.sitem_base;
+  const int copy = local / C.L.lt, t = local - copy * C.L.lt;
+  if (d.states[C.copy_base + copy].done != 0) return;
+  const double* partials = d.partials + 3 * (C.part_base + (size_t)copy * 2 * C.L.lt * C.nbx);
+  double f = 0.0, dd = 0.0, m = 0.0;
+  for (int j = threadIdx.x; j < 2 * C.nbx; j += blockDim.x) {
+    const int p = j / C.nbx, bx = j % C.nbx;
+    const double* q = partials + 3 * ((size_t)(p * C.L.lt + t) * C.nbx + bx);
+    f += q[0];
+    dd += q[1];
+    m = fmax(m, q[2]);
+  }
+  block_reduce3(f, dd, m, d.slice_sums + 3 * (C.slice_base + (size_t)copy * C.L.lt + t));
+}
+
+// per-copy totals and convergence bookkeeping, as final_reduce_kernel
+__global__ void check_batch_kernel(BDesc d, int ndir, int advance) {
+  int ci = 0;
+  while (ci + 1 < d.nconf && (int)blockIdx.x >= d.c[ci + 1].copy_base) ci++;
+  const BConf& C = d.c[ci];
+  const int copy = blockIdx.x - C.copy_base;
+  LoopState* S = d.states + blockIdx.x;
+  if (S->done != 0) return;
+  const double vol = 2.0 * (double)C.L.vh;
+  const double v3 = (double)C.L.lx * C.L.ly * C.L.lz;
+  reduce_and_check(d.slice_sums + 3 * (C.slice_base + (size_t)copy * C.L.lt), C.L.lt, vol, v3,
+                   ndir, d.reduced + blockIdx.x, S, nullptr, advance);
+}
+
+// continue the device loop while any copy is still running
+__global__ void continue_batch_kernel(BDesc d, int* running, cudaGraphConditionalHandle handle,
+                                      int use_handle) {
+  int n = 0;
+  for (int k = threadIdx.x; k < d.ncopies; k += blockDim.x) n += d.states[k].done == 0;
+  __shared__ int sh[32];
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += sh[w];
+    *running = tot;
+    if (use_handle) cudaGraphSetConditional(handle, tot > 0 ? 1u : 0u);
+  }
+}
+
+// FP64 <-> FP32 copies of every copy's g (g_32_to_64_kernel / g_64_to_32_kernel per copy)
+__global__ void convert_batch_kernel(BDesc d, int to64, int only_state) {
+  const int ci = conf_of(d, blockIdx.y, &BConf::copy_base);
+  const BConf& C = d.c[ci];
+  const int copy = blockIdx.y - C.copy_base;
+  if (only_state >= 0 && d.states[blockIdx.y].done != only_state) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C.L.vh) return;
+  const size_t vh = (size_t)C.L.vh;
+  for (int parity = 0; parity < 2; parity++) {
+    const float4* g32 = (const float4*)C.G32 + (size_t)copy * C.gstride32 + (size_t)parity * 3 * vh;
+    const double2* g64 = (const double2*)C.G64 + (size_t)copy * C.gstride64 + (size_t)parity * 6 * vh;
+    if (to64) {
+      Mat3<double> m;
+      Load<double, float, 12>::go(g32, vh, i, m);
+      Field<double, 12>::store((double2*)g64, vh, i, m);
+    } else {
+      Mat3<double> m;
+      Field<double, 12>::load(g64, vh, i, m);
+      Mat3<float> f;
+#pragma unroll
+      for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) f.e[r][c] = cmk<float>((float)m.e[r][c].re, (float)m.e[r][c].im);
+      Field<float, 12>::store((float4*)g32, vh, i, f);
+    }
+  }
+}
+
+}  // namespace gfx
+
+using namespace gfx;
+
+struct gfx_batch {
+  int nconf;
+  int ncopies;
+  int precision;
+  int K;
+  cudaStream_t stream;
+  bool own_stream;
+  std::vector<std::array<int, 4>> dims;
+  std::vector<int> copies;
+  BDesc desc;
+  int nitems, nmitems, nsitems;
+  std::vector<void*> allocs;
+  int* running;       // device
+  LoopState* h_states;  // pinned
+  std::vector<double> ms;
+  struct G {
+    int prec, ndir, ck;
+    double omega;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+  };
+  std::vector<G> graphs;
+  std::string err;
+};
+
+namespace {
+std::string g_batch_err;
+
+gfx_status bfail(gfx_batch* b, gfx_status s, const std::string& m) {
+  if (b) b->err = m;
+  g_batch_err = m;
+  return s;
+}
+
+#define BCK(call)                                                                          \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return bfail(b, GFX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+gfx_status balloc(gfx_batch* b, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return bfail(b, e == cudaErrorMemoryAllocation ? GFX_ERR_OOM : GFX_ERR_CUDA,
+                 std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  b->allocs.push_back(*p);
+  return GFX_OK;
+}
+
+size_t smem_bytes(int prec) { return (size_t)8 * (prec == 0 ? 3 : 6) * kBatchBlock * 16; }
+
+void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
+  const size_t sm = smem_bytes(prec);
+  for (int p = 0; p < 2; p++) {
+    if (prec == 0) {
+      if (ndir == 4)
+        or_batch_kernel<float, 4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+      else
+        or_batch_kernel<float, 3><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+    } else {
+      if (ndir == 4)
+        or_batch_kernel<double, 4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, omega);
+      else
+        or_batch_kernel<double, 3><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, omega);
+    }
+  }
+}
+
+void enqueue_check(gfx_batch* b, int cprec, int gprec, int ndir, int advance,
+                   unsigned long long handle, int use_handle) {
+  if (cprec == 0) {
+    if (ndir == 4) measure_batch_kernel<float, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    else measure_batch_kernel<float, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+  } else if (gprec == 0) {
+    if (ndir == 4) measure_batch_kernel<double, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    else measure_batch_kernel<double, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+  } else {
+    if (ndir == 4) measure_batch_kernel<double, double, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    else measure_batch_kernel<double, double, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+  }
+  slice_batch_kernel<<<b->nsitems, 256, 0, b->stream>>>(b->desc);
+  check_batch_kernel<<<b->ncopies, 256, 0, b->stream>>>(b->desc, ndir, advance);
+  continue_batch_kernel<<<1, 256, 0, b->stream>>>(b->desc, b->running,
+                                                 (cudaGraphConditionalHandle)handle, use_handle);
+}
+
+gfx_status read_states(gfx_batch* b) {
+  BCK(cudaMemcpyAsync(b->h_states, b->desc.states, sizeof(LoopState) * b->ncopies,
+                      cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+gfx_status write_states(gfx_batch* b) {
+  BCK(cudaMemcpyAsync(b->desc.states, b->h_states, sizeof(LoopState) * b->ncopies,
+                      cudaMemcpyHostToDevice, b->stream));
+  return GFX_OK;
+}
+
+gfx_status get_graph(gfx_batch* b, int prec, int ndir, int ck, double omega,
+                     cudaGraphExec_t* out) {
+  for (auto& g : b->graphs)
+    if (g.prec == prec && g.ndir == ndir && g.ck == ck && g.omega == omega) {
+      *out = g.exec;
+      return GFX_OK;
+    }
+  cudaGraph_t graph;
+  BCK(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle handle;
+  BCK(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.conditional.handle = handle;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  BCK(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  BCK(cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega);
+  enqueue_check(b, prec, prec, ndir, ck, (unsigned long long)handle, 1);
+  cudaGraph_t cap;
+  cudaError_t e = cudaStreamEndCapture(b->stream, &cap);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return bfail(b, GFX_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(e));
+  }
+  cudaGraphExec_t ex;
+  BCK(cudaGraphInstantiate(&ex, graph, 0));
+  b->graphs.push_back({prec, ndir, ck, omega, graph, ex});
+  *out = ex;
+  return GFX_OK;
+}
+
+// run the device loop of one phase until no copy is running
+gfx_status run_phase(gfx_batch* b, int prec, int ndir, int ck, double omega, int use_graph) {
+  if (use_graph) {
+    cudaGraphExec_t ex;
+    gfx_status s = get_graph(b, prec, ndir, ck, omega, &ex);
+    if (s) return s;
+    BCK(cudaGraphLaunch(ex, b->stream));
+    return read_states(b);
+  }
+  int running = 1;
+  while (running > 0) {
+    for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega);
+    enqueue_check(b, prec, prec, ndir, ck, 0, 0);
+    BCK(cudaGetLastError());
+    BCK(cudaMemcpyAsync(&running, b->running, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+  }
+  return read_states(b);
+}
+}  // namespace
+
+extern "C" {
+
+const char* gfx_batch_last_error(const gfx_batch* b) { return b ? b->err.c_str() : g_batch_err.c_str(); }
+
+gfx_status gfx_batch_destroy(gfx_batch* b) {
+  if (!b) return GFX_OK;
+  cudaStreamSynchronize(b->stream);
+  for (auto& g : b->graphs) {
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->h_states) cudaFreeHost(b->h_states);
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const int* ncopies,
+                            int precision, int copies_per_item, void* stream) {
+  gfx_batch* b = nullptr;
+  if (!out || !dims || !ncopies) return bfail(nullptr, GFX_ERR_ARG, "gfx_batch_create: NULL argument");
+  *out = nullptr;
+  if (nconf < 1 || nconf > kMaxConf)
+    return bfail(nullptr, GFX_ERR_ARG, "gfx_batch_create: 1..8 configurations");
+  if (precision < GFX_PREC_DOUBLE || precision > GFX_PREC_MIXED)
+    return bfail(nullptr, GFX_ERR_ARG, "gfx_batch_create: unknown precision");
+  for (int c = 0; c < nconf; c++) {
+    const int* d = dims + 4 * c;
+    if (d[0] < 2 || d[1] < 2 || d[2] < 2 || d[3] < 2 || (d[0] | d[1] | d[2] | d[3]) & 1)
+      return bfail(nullptr, GFX_ERR_BAD_VOLUME, "gfx_batch_create: extents must be even");
+    if ((long long)d[0] * d[1] * d[2] * d[3] / 2 > (1ll << 30) || ncopies[c] < 1)
+      return bfail(nullptr, GFX_ERR_ARG, "gfx_batch_create: volume or copy count");
+  }
+  b = new gfx_batch();
+  b->nconf = nconf;
+  b->precision = precision;
+  b->K = copies_per_item > 0 ? copies_per_item : 8;
+  b->running = nullptr;
+  b->h_states = nullptr;
+  std::memset((void*)&b->desc, 0, sizeof(b->desc));
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+    b->own_stream = false;
+  } else {
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete b;
+      return bfail(nullptr, GFX_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    b->own_stream = true;
+  }
+  gfx_status s;
+#define BTRY(x)          \
+  do {                   \
+    s = (x);             \
+    if (s) {             \
+      std::string m = b->err; \
+      gfx_batch_destroy(b); \
+      g_batch_err = m;   \
+      return s;          \
+    }                    \
+  } while (0)
+  int copy_base = 0, item = 0, mitem = 0, sitem = 0, slice = 0;
+  size_t part = 0;
+  for (int c = 0; c < nconf; c++) {
+    const int* d = dims + 4 * c;
+    BConf& C = b->desc.c[c];
+    C.L = make_lattice(d[0], d[1], d[2], d[3]);
+    b->dims.push_back({d[0], d[1], d[2], d[3]});
+    b->copies.push_back(ncopies[c]);
+    C.ncopies = ncopies[c];
+    C.copy_base = copy_base;
+    C.nblk = (C.L.vh + kBatchBlock - 1) / kBatchBlock;
+    C.ngroups = (C.ncopies + b->K - 1) / b->K;
+    C.item_base = item;
+    C.nbx = (C.L.st + kBatchBlock - 1) / kBatchBlock;
+    C.mitem_base = mitem;
+    C.sitem_base = sitem;
+    C.part_base = part;
+    C.slice_base = slice;
+    C.gstride32 = (size_t)2 * 3 * C.L.vh;
+    C.gstride64 = (size_t)2 * 6 * C.L.vh;
+    const size_t vh = C.L.vh;
+    void* p;
+    BTRY(balloc(b, &p, (size_t)8 * 6 * 16 * vh));
+    C.U64 = p;
+    BTRY(balloc(b, &p, (size_t)C.ncopies * C.gstride64 * 16));
+    C.G64 = p;
+    if (precision != GFX_PREC_DOUBLE) {
+      BTRY(balloc(b, &p, (size_t)8 * 3 * 16 * vh));
+      C.U32 = p;
+      BTRY(balloc(b, &p, (size_t)C.ncopies * C.gstride32 * 16));
+      C.G32 = p;
+    }
+    copy_base += C.ncopies;
+    item += C.nblk * C.ngroups;
+    mitem += C.ncopies * 2 * C.L.lt * C.nbx;
+    sitem += C.ncopies * C.L.lt;
+    slice += C.ncopies * C.L.lt;
+    part += (size_t)C.ncopies * 2 * C.L.lt * C.nbx;
+  }
+  b->ncopies = copy_base;
+  b->nitems = item;
+  b->nmitems = mitem;
+  b->nsitems = sitem;
+  b->desc.nconf = nconf;
+  b->desc.ncopies = copy_base;
+  b->desc.K = b->K;
+  void* p;
+  BTRY(balloc(b, &p, sizeof(LoopState) * copy_base));
+  b->desc.states = (LoopState*)p;
+  BTRY(balloc(b, &p, sizeof(double) * 3 * part));
+  b->desc.partials = (double*)p;
+  BTRY(balloc(b, &p, sizeof(double) * 3 * slice));
+  b->desc.slice_sums = (double*)p;
+  BTRY(balloc(b, &p, sizeof(Reduced) * copy_base));
+  b->desc.reduced = (Reduced*)p;
+  BTRY(balloc(b, &p, sizeof(int)));
+  b->running = (int*)p;
+  if (cudaMallocHost((void**)&b->h_states, sizeof(LoopState) * copy_base) != cudaSuccess) {
+    gfx_batch_destroy(b);
+    return bfail(nullptr, GFX_ERR_OOM, "cudaMallocHost failed");
+  }
+  std::memset(b->h_states, 0, sizeof(LoopState) * copy_base);
+  if (cudaFuncSetAttribute(or_batch_kernel<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_bytes(1)) != cudaSuccess ||
+      cudaFuncSetAttribute(or_batch_kernel<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem_bytes(1)) != cudaSuccess) {
+    cudaGetLastError();
+    gfx_batch_destroy(b);
+    return bfail(nullptr, GFX_ERR_CUDA, "cannot raise the shared-memory limit of the sweep kernel");
+  }
+#undef BTRY
+  *out = b;
+  return GFX_OK;
+}
+
+int gfx_batch_copies(const gfx_batch* b) { return b ? b->ncopies : 0; }
+
+static gfx_status copy_index(gfx_batch* b, int conf, int copy) {
+  if (!b || conf < 0 || conf >= b->nconf || copy < 0 || copy >= b->copies[conf])
+    return bfail(b, GFX_ERR_ARG, "configuration or copy index out of range");
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_set_links(gfx_batch* b, int conf, const double* su3) {
+  if (!b || !su3 || conf < 0 || conf >= b->nconf) return bfail(b, GFX_ERR_ARG, "bad argument");
+  BConf& C = b->desc.c[conf];
+  const size_t bytes = sizeof(double) * 18 * 4 * 2 * (size_t)C.L.vh;
+  double* scratch;
+  BCK(cudaMallocAsync((void**)&scratch, bytes, b->stream));
+  BCK(cudaMemcpyAsync(scratch, su3, bytes, cudaMemcpyHostToDevice, b->stream));
+  launch_pack_links(12, C.L, scratch, (void*)C.U64, b->stream);
+  if (C.U32) launch_convert_links_64_to_32(12, C.L, C.U64, (void*)C.U32, b->stream);
+  BCK(cudaFreeAsync(scratch, b->stream));
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_set_trafo(gfx_batch* b, int conf, int copy, const double* su3) {
+  gfx_status s = copy_index(b, conf, copy);
+  if (s) return s;
+  if (!su3) return bfail(b, GFX_ERR_ARG, "NULL trafo");
+  BConf& C = b->desc.c[conf];
+  const size_t bytes = sizeof(double) * 18 * 2 * (size_t)C.L.vh;
+  double* scratch;
+  BCK(cudaMallocAsync((void**)&scratch, bytes, b->stream));
+  BCK(cudaMemcpyAsync(scratch, su3, bytes, cudaMemcpyHostToDevice, b->stream));
+  launch_pack_g(1, C.L, scratch, (double2*)C.G64 + (size_t)copy * C.gstride64, b->stream);
+  BCK(cudaFreeAsync(scratch, b->stream));
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_get_trafo(gfx_batch* b, int conf, int copy, double* su3) {
+  gfx_status s = copy_index(b, conf, copy);
+  if (s) return s;
+  if (!su3) return bfail(b, GFX_ERR_ARG, "NULL trafo");
+  BConf& C = b->desc.c[conf];
+  const size_t bytes = sizeof(double) * 18 * 2 * (size_t)C.L.vh;
+  double* scratch;
+  BCK(cudaMallocAsync((void**)&scratch, bytes, b->stream));
+  launch_unpack_g(1, C.L, (const double2*)C.G64 + (size_t)copy * C.gstride64, scratch, b->stream);
+  BCK(cudaMemcpyAsync(su3, scratch, bytes, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaFreeAsync(scratch, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_random_haar(gfx_batch* b, uint64_t seed) {
+  if (!b) return bfail(nullptr, GFX_ERR_ARG, "NULL batch");
+  for (int c = 0; c < b->nconf; c++) {
+    BConf& C = b->desc.c[c];
+    for (int k = 0; k < C.ncopies; k++)
+      launch_haar_g(C.L, (double2*)C.G64 + (size_t)k * C.gstride64, seed + C.copy_base + k,
+                    b->stream);
+  }
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+
+gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_result* res,
+                               double* ms_out) {
+  if (!b || !pin) return bfail(b, GFX_ERR_ARG, "gfx_batch_overrelax: NULL argument");
+  gfx_or_params p = *pin;
+  if (p.maxit < 1 || p.checkinterval < 1) return bfail(b, GFX_ERR_ARG, "maxit, checkinterval");
+  if (p.checkinterval_double <= 0) p.checkinterval_double = p.checkinterval;
+  const int ndir = p.gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  const int prec0 = b->precision == GFX_PREC_DOUBLE ? 1 : 0;
+  const bool handover = b->precision == GFX_PREC_MIXED;
+  int maxvh = 0;
+  for (int c = 0; c < b->nconf; c++) maxvh = std::max(maxvh, b->desc.c[c].L.vh);
+  const dim3 cgrid((maxvh + 127) / 128, b->ncopies);
+  for (int k = 0; k < b->ncopies; k++) {
+    LoopState& H = b->h_states[k];
+    std::memset(&H, 0, sizeof(H));
+    H.ck = p.checkinterval;
+    H.maxit = p.maxit;
+    H.criterion = p.criterion;
+    H.phase = handover ? 0 : 1;
+    H.eps = p.eps;
+    H.switch_eps = p.switch_eps;
+    H.plateau_ratio = p.plateau_ratio > 0 ? p.plateau_ratio : 1e300;
+  }
+  gfx_status s = write_states(b);
+  if (s) return s;
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  BCK(cudaEventRecord(e0, b->stream));
+  // FP32 sweeps start from the FP32 copy of g (g_64_to_32 per copy)
+  if (prec0 == 0) convert_batch_kernel<<<cgrid, 128, 0, b->stream>>>(b->desc, 0, -1);
+  // iteration 0: sweep, then the first check (advance 0), as overrelax_gauge
+  enqueue_sweep(b, prec0, ndir, p.omega);
+  enqueue_check(b, prec0, prec0, ndir, 0, 0, 0);
+  BCK(cudaGetLastError());
+  if ((s = read_states(b))) return s;
+  auto any_running = [&]() {
+    for (int k = 0; k < b->ncopies; k++)
+      if (b->h_states[k].done == 0) return true;
+    return false;
+  };
+  if (any_running() && (s = run_phase(b, prec0, ndir, p.checkinterval, p.omega, p.use_graph)))
+    return s;
+  std::vector<int> iter_switch(b->ncopies, -1);
+  if (prec0 == 0) {
+    // widen every copy's g to FP64 (reunitarized)
+    convert_batch_kernel<<<cgrid, 128, 0, b->stream>>>(b->desc, 1, -1);
+    BCK(cudaGetLastError());
+  }
+  if (handover) {
+    // copies that left the FP32 phase are verified and polished in FP64
+    for (int k = 0; k < b->ncopies; k++) {
+      LoopState& H = b->h_states[k];
+      iter_switch[k] = H.iter;
+      if (H.done == 2) {
+        H.phase = 1;
+        H.done = 0;
+        H.prev = 0.0;
+        H.ck = p.checkinterval_double;
+      }
+    }
+    if ((s = write_states(b))) return s;
+    enqueue_check(b, 1, 1, ndir, 0, 0, 0);
+    BCK(cudaGetLastError());
+    if ((s = read_states(b))) return s;
+    if (any_running() &&
+        (s = run_phase(b, 1, ndir, p.checkinterval_double, p.omega, p.use_graph)))
+      return s;
+  }
+  BCK(cudaEventRecord(e1, b->stream));
+  BCK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms_out) *ms_out = ms;
+  int all = 1;
+  for (int c = 0; c < b->nconf; c++) {
+    const BConf& C = b->desc.c[c];
+    for (int k = 0; k < C.ncopies; k++) {
+      const int g = C.copy_base + k;
+      const LoopState& H = b->h_states[g];
+      const bool conv = H.done == 1;
+      all &= conv ? 1 : 0;
+      if (!res) continue;
+      gfx_copy_result& r = res[g];
+      r.conf = c;
+      r.copy = k;
+      r.converged = conv ? 1 : 0;
+      r.iterations = conv ? H.iter : -1;
+      r.sweeps = H.iter + 1;
+      if (b->precision == GFX_PREC_DOUBLE) r.sweeps_single = 0;
+      else if (!handover) r.sweeps_single = r.sweeps;
+      else r.sweeps_single = iter_switch[g] + 1;
+      r.sweeps_double = r.sweeps - r.sweeps_single;
+      r.F = H.last_F;
+      r.dAdA = H.last_dAdA;
+      r.maxdAdA = H.last_max;
+      r.theta = H.last_theta;
+      r.theta_slice_max = H.last_theta_slice_max;
+    }
+  }
+  return all ? GFX_OK : GFX_ERR_NOT_CONVERGED;
+}
+
+gfx_status gfx_batch_best(gfx_batch* b, const gfx_copy_result* res, int conf, int* best_copy,
+                          double* best_F) {
+  if (!b || !res || conf < 0 || conf >= b->nconf) return bfail(b, GFX_ERR_ARG, "bad argument");
+  const BConf& C = b->desc.c[conf];
+  int best = -1;
+  double bf = -1e300;
+  for (int k = 0; k < C.ncopies; k++) {
+    const gfx_copy_result& r = res[C.copy_base + k];
+    if (r.converged && r.F > bf) {
+      bf = r.F;
+      best = k;
+    }
+  }
+  if (best_copy) *best_copy = best;
+  if (best_F) *best_F = bf;
+  return best >= 0 ? GFX_OK : GFX_ERR_NOT_CONVERGED;
+}
+
+}  // extern "C"

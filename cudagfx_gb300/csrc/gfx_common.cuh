@@ -1,0 +1,204 @@
+// gfx_common.cuh -- device code shared by the single-lattice and batched kernels:
+// precision-converting loads, the star w(x), the per-site functional and the FP64
+// block reduction.  Sharing them keeps the batched results bit-identical per copy.
+#pragma once
+
+#include "gfx_device.cuh"
+#include "gfx_internal.h"
+
+namespace gfx {
+
+// ---------------------------------------------------------------------------
+// generic loads with precision conversion
+// ---------------------------------------------------------------------------
+template <typename TC, typename TS, int NR>
+struct Load {
+  typedef typename VecOf<TS>::type V;
+  __device__ static __forceinline__ void go(const V* base, size_t stride, int i, Mat3<TC>& m) {
+    Field<TC, NR>::load(base, stride, i, m);
+  }
+};
+// FP64 compute on FP32-stored g: widen rows 0,1 and reunitarize in FP64
+template <>
+struct Load<double, float, 12> {
+  __device__ static __forceinline__ void go(const float4* base, size_t stride, int i,
+                                            Mat3<double>& m) {
+    Mat3<float> f;
+    Field<float, 12>::load(base, stride, i, f);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int c = 0; c < 3; c++) m.e[r][c] = cmk<double>(f.e[r][c].re, f.e[r][c].im);
+    normalize<double, true>(m);
+  }
+};
+
+// star w(x) = sum_mu U_mu(x) g^+(x+mu) + U_mu^+(x-mu) g^+(x-mu)   (overrelax.cu:350-394)
+template <typename TC, typename TSU, int NRU, typename TSG, int NRG, int NDIR>
+__device__ __forceinline__ void compute_star(const Lattice& L, const Site& c, int parity,
+                                             const typename VecOf<TSU>::type* __restrict__ U,
+                                             const typename VecOf<TSG>::type* __restrict__ G,
+                                             Mat3<TC>& star) {
+  constexpr int NCU = Field<TSU, NRU>::NCHUNK;
+  constexpr int NCG = Field<TSG, NRG>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  const int q = 1 - parity;
+  const typename VecOf<TSG>::type* Gq = G + (size_t)q * NCG * vh;
+  mzero(star);
+#pragma unroll
+  for (int mu = 0; mu < NDIR; mu++) {
+    Mat3<TC> a, b;
+    Load<TC, TSU, NRU>::go(U + (size_t)(parity * 4 + mu) * NCU * vh, vh, c.i, a);
+    const int jf = nb_fwd(L, c, mu);
+    Load<TC, TSG, NRG>::go(Gq, vh, jf, b);
+    addmul_nd(star, a, b);
+    const int jb = nb_bwd(L, c, mu);
+    Load<TC, TSU, NRU>::go(U + (size_t)(q * 4 + mu) * NCU * vh, vh, jb, a);
+    Load<TC, TSG, NRG>::go(Gq, vh, jb, b);
+    addmul_dd(star, a, b);
+  }
+}
+
+// Per-site functional from X = g w (overrelax.cu:451-605, see measure_kernel):
+// f = Re tr X, d = tr[Delta Delta^+] = sum_ij |AH(X)_ij|^2.
+template <typename TC>
+__device__ __forceinline__ void site_functional(const Mat3<TC>& g, const Mat3<TC>& star,
+                                                double& f, double& d) {
+  Mat3<TC> X;
+  mul(X, g, star);
+  f = (double)X.e[0][0].re + (double)X.e[1][1].re + (double)X.e[2][2].re;
+  const TC tim = (X.e[0][0].im + X.e[1][1].im + X.e[2][2].im) * TC(1.0 / 3.0);
+  TC acc = TC(0);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const TC di = X.e[a][a].im - tim;
+    acc += di * di;
+  }
+  TC off = TC(0);
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = a + 1; b < 3; b++) {
+      const TC re = (X.e[a][b].re - X.e[b][a].re) * TC(0.5);
+      const TC im = (X.e[a][b].im + X.e[b][a].im) * TC(0.5);
+      off += re * re + im * im;
+    }
+  d = (double)acc + 2.0 * (double)off;
+}
+
+// FP64 sums of f and d and max of m over the block, in a fixed order
+__device__ __forceinline__ void block_reduce3(double f, double d, double m, double* out) {
+  __shared__ double sh[3][32];
+  f = warp_sum(f);
+  d = warp_sum(d);
+  m = warp_max(m);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = f;
+    sh[1][w] = d;
+    sh[2][w] = m;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    f = l < nw ? sh[0][l] : 0.0;
+    d = l < nw ? sh[1][l] : 0.0;
+    m = l < nw ? sh[2][l] : 0.0;
+    f = warp_sum(f);
+    d = warp_sum(d);
+    m = warp_max(m);
+    if (l == 0) {
+      out[0] = f;
+      out[1] = d;
+      out[2] = m;
+    }
+  }
+}
+
+enum { CRIT_MAXDADA = 0, CRIT_THETA = 1, CRIT_THETA_SLICES = 2 };
+
+// Totals over the slices, then (when loop is given) one check of the convergence loop:
+// record, compare with the criterion, decide done (0 run on, 1 converged, 2 leave the
+// FP32 phase, 3 iteration cap).  Called by all threads of one block; returns done on
+// thread 0 (and -1 elsewhere).
+__device__ __forceinline__ int reduce_and_check(const double* slice_sums, int lt, double vol,
+                                                double v3, int ndir, Reduced* out,
+                                                LoopState* loop, CheckRecord* hist,
+                                                int advance) {
+  double f = 0.0, d = 0.0, m = 0.0, tmax = 0.0;
+  for (int t = threadIdx.x; t < lt; t += blockDim.x) {
+    f += slice_sums[3 * t];
+    d += slice_sums[3 * t + 1];
+    m = fmax(m, slice_sums[3 * t + 2]);
+    tmax = fmax(tmax, slice_sums[3 * t + 1] / (3.0 * v3));
+  }
+  // one warp suffices for lt <= 32*k; reduce in a fixed order
+  __shared__ double sh[4][32];
+  f = warp_sum(f);
+  d = warp_sum(d);
+  m = warp_max(m);
+  tmax = warp_max(tmax);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = f;
+    sh[1][w] = d;
+    sh[2][w] = m;
+    sh[3][w] = tmax;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return -1;
+  f = d = m = tmax = 0.0;
+  for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+    f += sh[0][k];
+    d += sh[1][k];
+    m = fmax(m, sh[2][k]);
+    tmax = fmax(tmax, sh[3][k]);
+  }
+  Reduced r;
+  r.F = f / (2.0 * ndir * vol);
+  r.dAdA = d / vol;
+  r.maxdAdA = m;
+  r.theta = r.dAdA / 3.0;
+  r.theta_slice_max = tmax;
+  *out = r;
+  if (!loop) return 0;
+  LoopState& S = *loop;
+  S.iter += advance;
+  const double value = S.criterion == CRIT_MAXDADA ? r.maxdAdA
+                       : S.criterion == CRIT_THETA ? r.theta
+                                                   : r.theta_slice_max;
+  if (S.nhist < S.hist_cap && hist) {
+    CheckRecord& h = hist[S.nhist];
+    h.iter = S.iter;
+    h.phase = S.phase;
+    h.F = r.F;
+    h.dAdA = r.dAdA;
+    h.maxdAdA = r.maxdAdA;
+    h.theta = r.theta;
+    h.theta_slice_max = r.theta_slice_max;
+  }
+  S.nhist++;
+  S.last_F = r.F;
+  S.last_dAdA = r.dAdA;
+  S.last_max = r.maxdAdA;
+  S.last_theta = r.theta;
+  S.last_theta_slice_max = r.theta_slice_max;
+  int done = 0;
+  if (S.phase == 0) {
+    // single-precision phase: hand over to the double-precision phase when the target
+    // is reached (the FP64 phase verifies it), or when, below switch_eps, the value
+    // stops decreasing -- the FP32 rounding floor, which a few FP64 sweeps remove
+    if (value < S.eps ||
+        (value < S.switch_eps && S.prev > 0.0 && value > S.plateau_ratio * S.prev))
+      done = 2;
+  } else if (value < S.eps) {
+    done = 1;
+  }
+  if (!done && S.iter + S.ck >= S.maxit) done = 3;
+  S.prev = value;
+  S.done = done;
+  return done;
+}
+
+
+}  // namespace gfx

@@ -66,6 +66,8 @@ void launch_convert_links_64_to_32(int link_nr, const Lattice& L, const void* U6
 void launch_convert_g(int from_prec, int to_prec, const Lattice& L, const void* Gin, void* Gout,
                       cudaStream_t s);
 void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s);
+// Haar-random FP64 g: the value at lexicographic site pos depends only on (seed, pos)
+void launch_haar_g(const Lattice& L, double2* G64, unsigned long long seed, cudaStream_t s);
 
 // ----- heatbath family (gfx_heatbath.cu) -----
 void launch_sa_heatbath(int prec, int link_nr, const Lattice& L, const void* U, void* G,

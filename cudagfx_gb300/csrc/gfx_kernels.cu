@@ -2,6 +2,7 @@
 // plaquette, Polyakov loop and field-layout kernels for sm_103a.
 #include <cstdio>
 
+#include "gfx_common.cuh"
 #include "gfx_internal.h"
 
 namespace gfx {
@@ -31,57 +32,6 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
   L.d_ly = mk((uint32_t)ly);
   L.d_lz = mk((uint32_t)lz);
   return L;
-}
-
-// ---------------------------------------------------------------------------
-// generic loads with precision conversion
-// ---------------------------------------------------------------------------
-template <typename TC, typename TS, int NR>
-struct Load {
-  typedef typename VecOf<TS>::type V;
-  __device__ static __forceinline__ void go(const V* base, size_t stride, int i, Mat3<TC>& m) {
-    Field<TC, NR>::load(base, stride, i, m);
-  }
-};
-// FP64 compute on FP32-stored g: widen rows 0,1 and reunitarize in FP64
-template <>
-struct Load<double, float, 12> {
-  __device__ static __forceinline__ void go(const float4* base, size_t stride, int i,
-                                            Mat3<double>& m) {
-    Mat3<float> f;
-    Field<float, 12>::load(base, stride, i, f);
-#pragma unroll
-    for (int r = 0; r < 2; r++)
-#pragma unroll
-      for (int c = 0; c < 3; c++) m.e[r][c] = cmk<double>(f.e[r][c].re, f.e[r][c].im);
-    normalize<double, true>(m);
-  }
-};
-
-// star w(x) = sum_mu U_mu(x) g^+(x+mu) + U_mu^+(x-mu) g^+(x-mu)   (overrelax.cu:350-394)
-template <typename TC, typename TSU, int NRU, typename TSG, int NRG, int NDIR>
-__device__ __forceinline__ void compute_star(const Lattice& L, const Site& c, int parity,
-                                             const typename VecOf<TSU>::type* __restrict__ U,
-                                             const typename VecOf<TSG>::type* __restrict__ G,
-                                             Mat3<TC>& star) {
-  constexpr int NCU = Field<TSU, NRU>::NCHUNK;
-  constexpr int NCG = Field<TSG, NRG>::NCHUNK;
-  const size_t vh = (size_t)L.vh;
-  const int q = 1 - parity;
-  const typename VecOf<TSG>::type* Gq = G + (size_t)q * NCG * vh;
-  mzero(star);
-#pragma unroll
-  for (int mu = 0; mu < NDIR; mu++) {
-    Mat3<TC> a, b;
-    Load<TC, TSU, NRU>::go(U + (size_t)(parity * 4 + mu) * NCU * vh, vh, c.i, a);
-    const int jf = nb_fwd(L, c, mu);
-    Load<TC, TSG, NRG>::go(Gq, vh, jf, b);
-    addmul_nd(star, a, b);
-    const int jb = nb_bwd(L, c, mu);
-    Load<TC, TSU, NRU>::go(U + (size_t)(q * 4 + mu) * NCU * vh, vh, jb, a);
-    Load<TC, TSG, NRG>::go(Gq, vh, jb, b);
-    addmul_dd(star, a, b);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -137,34 +87,6 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
 // vector potential.  Each block covers part of one time slice of one parity and
 // writes (sum F, sum dAdA, max dAdA).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void block_reduce3(double f, double d, double m, double* out) {
-  __shared__ double sh[3][32];
-  f = warp_sum(f);
-  d = warp_sum(d);
-  m = warp_max(m);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-    sh[0][w] = f;
-    sh[1][w] = d;
-    sh[2][w] = m;
-  }
-  __syncthreads();
-  if (w == 0) {
-    const int nw = blockDim.x >> 5;
-    f = l < nw ? sh[0][l] : 0.0;
-    d = l < nw ? sh[1][l] : 0.0;
-    m = l < nw ? sh[2][l] : 0.0;
-    f = warp_sum(f);
-    d = warp_sum(d);
-    m = warp_max(m);
-    if (l == 0) {
-      out[0] = f;
-      out[1] = d;
-      out[2] = m;
-    }
-  }
-}
-
 template <typename TC, typename TSU, int NRU, typename TSG, int NDIR>
 __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
                                                        const typename VecOf<TSU>::type* U,
@@ -180,26 +102,7 @@ __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
     compute_star<TC, TSU, NRU, TSG, 12, NDIR>(L, c, parity, U, G, star);
     constexpr int NCG = Field<TSG, 12>::NCHUNK;
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * L.vh, (size_t)L.vh, i, g);
-    Mat3<TC> X;
-    mul(X, g, star);
-    f = (double)X.e[0][0].re + (double)X.e[1][1].re + (double)X.e[2][2].re;
-    const TC tim = (X.e[0][0].im + X.e[1][1].im + X.e[2][2].im) * TC(1.0 / 3.0);
-    TC acc = TC(0);
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      const TC di = X.e[a][a].im - tim;
-      acc += di * di;
-    }
-    TC off = TC(0);
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = a + 1; b < 3; b++) {
-        const TC re = (X.e[a][b].re - X.e[b][a].re) * TC(0.5);
-        const TC im = (X.e[a][b].im + X.e[b][a].im) * TC(0.5);
-        off += re * re + im * im;
-      }
-    d = (double)acc + 2.0 * (double)off;
+    site_functional(g, star, f, d);
   }
   const int nbx = gridDim.x;
   block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + blockIdx.x));
@@ -251,87 +154,13 @@ __global__ void slice_reduce_kernel(const double* partials, int nbx, int lt, dou
   block_reduce3(f, d, m, slice_sums + 3 * t);
 }
 
-enum { CRIT_MAXDADA = 0, CRIT_THETA = 1, CRIT_THETA_SLICES = 2 };
-
 __global__ void final_reduce_kernel(const double* slice_sums, int lt, double vol, double v3,
                                     int ndir, Reduced* out, LoopState* loop, CheckRecord* hist,
                                     int advance, cudaGraphConditionalHandle handle,
                                     int use_handle) {
-  __shared__ double smax_theta;
-  double f = 0.0, d = 0.0, m = 0.0, tmax = 0.0;
-  for (int t = threadIdx.x; t < lt; t += blockDim.x) {
-    f += slice_sums[3 * t];
-    d += slice_sums[3 * t + 1];
-    m = fmax(m, slice_sums[3 * t + 2]);
-    tmax = fmax(tmax, slice_sums[3 * t + 1] / (3.0 * v3));
-  }
-  // one warp suffices for lt <= 32*k; reduce in a fixed order
-  __shared__ double sh[4][32];
-  f = warp_sum(f);
-  d = warp_sum(d);
-  m = warp_max(m);
-  tmax = warp_max(tmax);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) {
-    sh[0][w] = f;
-    sh[1][w] = d;
-    sh[2][w] = m;
-    sh[3][w] = tmax;
-  }
-  __syncthreads();
-  if (threadIdx.x != 0) return;
-  f = d = m = tmax = 0.0;
-  for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-    f += sh[0][k];
-    d += sh[1][k];
-    m = fmax(m, sh[2][k]);
-    tmax = fmax(tmax, sh[3][k]);
-  }
-  (void)smax_theta;
-  Reduced r;
-  r.F = f / (2.0 * ndir * vol);
-  r.dAdA = d / vol;
-  r.maxdAdA = m;
-  r.theta = r.dAdA / 3.0;
-  r.theta_slice_max = tmax;
-  *out = r;
-  if (!loop) return;
-  LoopState& S = *loop;
-  S.iter += advance;
-  const double value = S.criterion == CRIT_MAXDADA ? r.maxdAdA
-                       : S.criterion == CRIT_THETA ? r.theta
-                                                   : r.theta_slice_max;
-  if (S.nhist < S.hist_cap && hist) {
-    CheckRecord& h = hist[S.nhist];
-    h.iter = S.iter;
-    h.phase = S.phase;
-    h.F = r.F;
-    h.dAdA = r.dAdA;
-    h.maxdAdA = r.maxdAdA;
-    h.theta = r.theta;
-    h.theta_slice_max = r.theta_slice_max;
-  }
-  S.nhist++;
-  S.last_F = r.F;
-  S.last_dAdA = r.dAdA;
-  S.last_max = r.maxdAdA;
-  S.last_theta = r.theta;
-  S.last_theta_slice_max = r.theta_slice_max;
-  int done = 0;
-  if (S.phase == 0) {
-    // single-precision phase: hand over to the double-precision phase when the target
-    // is reached (the FP64 phase verifies it), or when, below switch_eps, the value
-    // stops decreasing -- the FP32 rounding floor, which a few FP64 sweeps remove
-    if (value < S.eps ||
-        (value < S.switch_eps && S.prev > 0.0 && value > S.plateau_ratio * S.prev))
-      done = 2;
-  } else if (value < S.eps) {
-    done = 1;
-  }
-  if (!done && S.iter + S.ck >= S.maxit) done = 3;
-  S.prev = value;
-  S.done = done;
-  if (use_handle) cudaGraphSetConditional(handle, done == 0 ? 1u : 0u);
+  const int done = reduce_and_check(slice_sums, lt, vol, v3, ndir, out, loop, hist, advance);
+  if (threadIdx.x == 0 && loop && use_handle)
+    cudaGraphSetConditional(handle, done == 0 ? 1u : 0u);
 }
 
 void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
@@ -687,6 +516,40 @@ __global__ void apply_trafo_kernel(Lattice L, double2* U, const double2* G) {
     addmul_nd(r, h, gn);
     Field<double, NR>::store(blk, vh, i, r);
   }
+}
+
+// Haar SU(3): rows 0,1 of a complex Gaussian matrix, Gram-Schmidt; the Gaussians come
+// from splitmix64 streams keyed by (seed, lexicographic site) and Box-Muller in FP64
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long& x) {
+  unsigned long long z = (x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__global__ void haar_g_kernel(Lattice L, double2* G, unsigned long long seed) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  const long long pos = lexi_of(L, i, parity);
+  unsigned long long st = seed * 0xD1B54A32D192ED03ull + (unsigned long long)pos * 0x8CB92BA72F3D8DD7ull;
+  Mat3<double> m;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const double u1 = ((double)(splitmix64(st) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double u2 = ((double)(splitmix64(st) >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    const double r = sqrt(-2.0 * log(u1));
+    double sp, cp;
+    sincospi(2.0 * u2, &sp, &cp);
+    m.e[k / 3][k % 3] = cmk(r * cp, r * sp);
+  }
+  normalize<double, false>(m);
+  Field<double, 12>::store(G + (size_t)parity * 6 * L.vh, (size_t)L.vh, i, m);
+}
+
+void launch_haar_g(const Lattice& L, double2* G64, unsigned long long seed, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  haar_g_kernel<<<grid, 128, 0, s>>>(L, G64, seed);
 }
 
 void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s) {

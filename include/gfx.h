@@ -216,6 +216,41 @@ gfx_status gfx_thermalize(gfx_ctx *ctx, const gfx_therm_params *p, double *plaq,
 gfx_status gfx_link_heatbath_halfsweep(gfx_ctx *ctx, int parity, int nu, double beta,
                                        int variant);
 
+/* ---- batched Gribov copies (no counterpart in the reference: its main fixes one
+ * copy per run, cudagaugefix.cu:706-821) ---- */
+typedef struct gfx_batch gfx_batch;
+
+typedef struct {
+  int conf, copy;
+  int converged;
+  int iterations;     /* as overrelax_gauge: converging check's iteration, or -1 */
+  int sweeps, sweeps_single, sweeps_double;
+  double F, dAdA, maxdAdA, theta, theta_slice_max;
+} gfx_copy_result;
+
+/* nconf configurations with extents dims[4*c..4*c+3] and ncopies[c] gauge copies each
+ * (at most 8 configurations); copies_per_item = copies updated per staged set of links
+ * (0: 8) */
+gfx_status gfx_batch_create(gfx_batch **out, int nconf, const int *dims, const int *ncopies,
+                            int precision, int copies_per_item, void *stream);
+gfx_status gfx_batch_destroy(gfx_batch *b);
+const char *gfx_batch_last_error(const gfx_batch *b);
+int gfx_batch_copies(const gfx_batch *b);
+gfx_status gfx_batch_set_links(gfx_batch *b, int conf, const double *su3_links);
+gfx_status gfx_batch_set_trafo(gfx_batch *b, int conf, int copy, const double *su3_trafo);
+gfx_status gfx_batch_get_trafo(gfx_batch *b, int conf, int copy, double *su3_trafo);
+/* Haar-random start for every copy: copy k of configuration c (global index
+ * copy_base(c) + k) uses seed + global index (same generator as gfx_random_trafo_haar) */
+gfx_status gfx_batch_random_haar(gfx_batch *b, uint64_t seed);
+/* fix every copy (one device loop for the whole batch); results[gfx_batch_copies()] */
+gfx_status gfx_batch_overrelax(gfx_batch *b, const gfx_or_params *p, gfx_copy_result *results,
+                               double *ms);
+/* the converged copy of configuration conf with the largest functional */
+gfx_status gfx_batch_best(gfx_batch *b, const gfx_copy_result *results, int conf,
+                          int *best_copy, double *best_F);
+/* Haar-random g on the device, g(site) from a counter-based stream of (seed, site) */
+gfx_status gfx_random_trafo_haar(gfx_ctx *ctx, uint64_t seed);
+
 /* ---- host-side helpers ---- */
 /* page-locked host memory for the field copies (cudaMallocHost); NULL on failure */
 void *gfx_host_alloc(size_t bytes);

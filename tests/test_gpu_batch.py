@@ -1,0 +1,56 @@
+"""Batched Gribov copies: every copy of every configuration, fixed together in one
+device loop, follows the same trajectory as the same start fixed alone (same check
+iterations, same FP32/FP64 sweep split, same functional to 1e-13)."""
+import numpy as np
+import pytest
+
+from conftest import smooth_links
+
+pytestmark = pytest.mark.gpu
+
+DIMS = [(8, 8, 8, 8), (4, 6, 8, 10)]
+
+
+def _batch(gfx, prec, ncopies, K, seed=900):
+    b = gfx.Batch(DIMS, ncopies, precision=prec, copies_per_item=K)
+    links = [smooth_links(d, 0.3 + 0.1 * c, 50 + c) for c, d in enumerate(DIMS)]
+    for c, u in enumerate(links):
+        b.set_links(c, u)
+    b.random_haar(seed)
+    return b, links
+
+
+@pytest.mark.parametrize("prec,K", [(2, 8), (2, 2), (0, 3)])
+def test_batch_copies_match_single_contexts(gfx, prec, K):
+    ncopies = [5, 3]
+    b, links = _batch(gfx, prec, ncopies, K)
+    kw = dict(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA,
+              switch_eps=1e-9, checkinterval_double=5)
+    res, ms = b.overrelax(**kw)
+    assert all(r["converged"] for r in res)
+    base = 0
+    for c, dims in enumerate(DIMS):
+        ctx = gfx.Context(dims, precision=prec)
+        ctx.set_links(links[c])
+        for k in range(ncopies[c]):
+            ctx.random_trafo_haar(900 + base + k)
+            r = ctx.overrelax(**kw)
+            got = res[base + k]
+            assert (got["conf"], got["copy"]) == (c, k)
+            assert got["iterations"] == r.iterations
+            assert got["sweeps_single"] == r.sweeps_single
+            assert got["sweeps_double"] == r.sweeps_double
+            assert got["F"] == pytest.approx(r.final_values.F, rel=1e-13)
+            assert got["theta"] == pytest.approx(r.final_values.theta, rel=1e-9)
+            g_single = ctx.get_trafo()
+            assert np.max(np.abs(b.get_trafo(c, k) - g_single)) < 1e-12
+        base += ncopies[c]
+
+
+def test_batch_best_copy(gfx):
+    b, links = _batch(gfx, 2, [6, 2], 4)
+    res, _ = b.overrelax(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7,
+                         criterion=gfx.CRIT_THETA)
+    k, f = b.best(0)
+    fs = [r["F"] for r in res[:6]]
+    assert k == int(np.argmax(fs)) and f == max(fs)
