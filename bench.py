@@ -63,10 +63,69 @@ def parse():
                     help="host-driven check loop instead of the CUDA-graph while loop (same "
                          "kernels; profilers list each launch)")
     ap.add_argument("--cpu-sweeps", type=int, default=0, help="CPU sample sweeps (0: auto)")
+    ap.add_argument("--no-gribov", action="store_true",
+                    help="skip the batched-Gribov-copies measurement")
+    ap.add_argument("--gribov-copies", default="64,32",
+                    help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
     ap.add_argument("--kernels", action="store_true",
                     help="no timing: a few launches of each hot kernel on the lattice, for "
                          "ncu captures")
     return ap.parse_args()
+
+
+def gribov_batch(args, gfx, mt_source):
+    """Batched Gribov copies: 64 copies of a 16^4 beta=6.0 configuration and 32 copies of
+    a 24^4 beta=6.2 configuration, Haar-random starts (seed 2024 + copy), mixed FP32->FP64
+    OR omega=1.7 to theta<1e-12, the largest-functional copy kept per configuration.
+    Batched: one device loop for all copies.  Sequential: the same starts, one
+    single-lattice solve per copy.  Both timed with CUDA events (solve only)."""
+    confs = [((16, 16, 16, 16), 6.0), ((24, 24, 24, 24), 6.2)]
+    ncopies = [int(x) for x in args.gribov_copies.split(",")]
+    kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval, omega=args.omega,
+              criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
+              checkinterval_double=args.checkinterval_double)
+    links = []
+    for k, (d, beta) in enumerate(confs):
+        V = int(np.prod(d))
+        c = gfx.Context(d)
+        c.set_links(gfx.unit_init(4 * V))
+        mt_source(c)
+        c.mt_seed(100 + k)
+        c.mt_init(2 * V, 8 * V)
+        c.thermalize(beta, args.therm, variant=gfx.HB_KENNEDY_PENDLETON)
+        links.append(c.get_links())
+        c.close()
+    b = gfx.Batch([d for d, _ in confs], ncopies, precision=gfx.PREC_MIXED)
+    for k, u in enumerate(links):
+        b.set_links(k, u)
+    b.random_haar(2024)
+    b.overrelax(**kw)  # warm-up (graph instantiation)
+    b.random_haar(2024)
+    res, ms_b = b.overrelax(**kw)
+    best = [b.best(k) for k in range(len(confs))]
+    upd = sum(r["sweeps"] * int(np.prod(confs[r["conf"]][0])) for r in res)
+    b.close()
+    ms_s, base, upd_s = 0.0, 0, 0
+    for k, (d, _) in enumerate(confs):
+        c = gfx.Context(d, precision=gfx.PREC_MIXED)
+        c.set_links(links[k])
+        c.random_trafo_haar(2024 + base)
+        c.overrelax(**kw)  # warm-up
+        for j in range(ncopies[k]):
+            c.random_trafo_haar(2024 + base + j)
+            r = c.overrelax(**kw)
+            ms_s += r.ms
+            upd_s += r.sweeps * int(np.prod(d))
+        base += ncopies[k]
+        c.close()
+    return {"workload": "%d x 16^4 (beta 6.0) + %d x 24^4 (beta 6.2) Gribov copies, Haar starts, "
+                        "theta<%g" % (ncopies[0], ncopies[1], args.eps),
+            "converged": sum(r["converged"] for r in res), "copies": len(res),
+            "batched_s": ms_b / 1000.0, "sequential_s": ms_s / 1000.0,
+            "batched_site_updates_per_s": upd / (ms_b / 1000.0),
+            "sequential_site_updates_per_s": upd_s / (ms_s / 1000.0),
+            "throughput_ratio": (upd / (ms_b / 1000.0)) / (upd_s / (ms_s / 1000.0)),
+            "best_copy": [{"copy": k, "F": f} for k, f in best]}
 
 
 def run_kernels(args, dims):
@@ -282,10 +341,14 @@ def run_gfx(args, dims):
     ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
     ctx.set_links(gfx.unit_init(4 * V))
     dat = mt_params_path()
-    if dat:
-        ctx.mt_load_file(dat)
-    else:
-        ctx.mt_load_params(synthetic_mt_params())
+
+    def mt_source(c):
+        if dat:
+            c.mt_load_file(dat)
+        else:
+            c.mt_load_params(synthetic_mt_params())
+
+    mt_source(ctx)
     ctx.mt_seed(42 + rank)
     ctx.mt_init(2 * V, 8 * V)
     t0 = time.perf_counter()
@@ -381,6 +444,7 @@ def run_gfx(args, dims):
                "sample": "%d OR sweeps of %s (%.1f s), CPU restatement of the reference update, "
                          "OpenMP over one parity" % (cs, "x".join(map(str, dims)), dt)}
     ctx.close()
+    gribov = None if args.no_gribov else gribov_batch(args, gfx, mt_source)
     if rank != 0:
         return
     h2d = pin_links.nbytes + pin_g0.nbytes
@@ -411,6 +475,7 @@ def run_gfx(args, dims):
                 "d2h_bytes_per_step": pin_out.nbytes},
         "clocks": clocks,
         "gpu_launches": int(launches),
+        "gribov_batch": gribov,
     }
     print(json.dumps(out), flush=True)
 

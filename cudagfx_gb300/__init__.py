@@ -432,7 +432,7 @@ class CopyResult(_c.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-_sig("gfx_batch_create", _I, [_c.POINTER(_V), _I, _c.POINTER(_I), _c.POINTER(_I), _I, _I, _V])
+_sig("gfx_batch_create", _I, [_c.POINTER(_V), _I, _c.POINTER(_I), _c.POINTER(_I), _I, _V])
 _sig("gfx_batch_destroy", _I, [_V])
 _sig("gfx_batch_last_error", _c.c_char_p, [_V])
 _sig("gfx_batch_copies", _I, [_V])
@@ -448,12 +448,12 @@ _sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])
 class Batch:
     """Gauge copies of several configurations fixed together (gfx_batch_*)."""
 
-    def __init__(self, dims_list, ncopies, precision=PREC_MIXED, copies_per_item=0, stream=None):
+    def __init__(self, dims_list, ncopies, precision=PREC_MIXED, stream=None):
         n = len(dims_list)
         d = (_I * (4 * n))(*[x for dims in dims_list for x in dims])
         c = (_I * n)(*ncopies)
         h = _V()
-        s = lib.gfx_batch_create(_c.byref(h), n, d, c, precision, copies_per_item,
+        s = lib.gfx_batch_create(_c.byref(h), n, d, c, precision,
                                  _V(stream) if stream else None)
         if s != 0:
             raise GfxError(s, lib.gfx_batch_last_error(None).decode())

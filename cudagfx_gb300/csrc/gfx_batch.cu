@@ -3,9 +3,9 @@
 // A batch holds nconf configurations (each with its own lattice extents and links) and
 // ncopies[c] gauge transformations per configuration (Gribov copies).  Every half-sweep
 // of every active copy of every configuration is one kernel launch: a work item is
-// (configuration, block of 128 sites, group of K copies).  The item's threads stage
-// the 8 links of their site (4 forward, 4 backward) once in shared memory and update
-// the K copies with them, so each link read from HBM serves K copy updates.  The
+// (configuration, block of 128 sites, copy), ordered copy-minor, so the copies of a site
+// block run side by side and share its links through L2 -- each link read from HBM
+// serves all copies of its configuration.  The
 // checks, their per-copy reductions and the per-copy convergence bookkeeping run on
 // the device; the whole loop is one CUDA graph with a conditional while node, as for a
 // single lattice.  Per copy, the arithmetic and the reduction order are those of the
@@ -37,7 +37,6 @@ struct BConf {
   int copy_base;     // index of copy 0 among all copies of the batch
   int item_base;     // first sweep work item
   int nblk;          // site blocks per parity
-  int ngroups;       // copy groups of K
   int mitem_base;    // first measurement item
   int nbx;           // measurement blocks per time slice
   size_t part_base;  // first partial triple of copy 0 (copy k: + k * 2 * lt * nbx)
@@ -49,7 +48,6 @@ struct BDesc {
   BConf c[kMaxConf];
   int nconf;
   int ncopies;  // all configurations
-  int K;        // copies per sweep item
   LoopState* states;
   double* partials;
   double* slice_sums;
@@ -62,95 +60,37 @@ __device__ __forceinline__ int conf_of(const BDesc& d, int item, int BConf::*bas
   return ci;
 }
 
-template <typename T>
-__device__ __forceinline__ void smem_load12(const typename VecOf<T>::type* sl, int link, int tid,
-                                            Mat3<T>& m);
-template <>
-__device__ __forceinline__ void smem_load12<float>(const float4* sl, int link, int tid,
-                                                   Mat3<float>& m) {
-  const float4 a = sl[(link * 3 + 0) * kBatchBlock + tid];
-  const float4 b = sl[(link * 3 + 1) * kBatchBlock + tid];
-  const float4 c = sl[(link * 3 + 2) * kBatchBlock + tid];
-  m.e[0][0] = cmk(a.x, a.y);
-  m.e[0][1] = cmk(a.z, a.w);
-  m.e[0][2] = cmk(b.x, b.y);
-  m.e[1][0] = cmk(b.z, b.w);
-  m.e[1][1] = cmk(c.x, c.y);
-  m.e[1][2] = cmk(c.z, c.w);
-  row2_from_01(m);
-}
-template <>
-__device__ __forceinline__ void smem_load12<double>(const double2* sl, int link, int tid,
-                                                    Mat3<double>& m) {
-#pragma unroll
-  for (int k = 0; k < 6; k++) {
-    const double2 v = sl[(link * 6 + k) * kBatchBlock + tid];
-    m.e[k / 3][k % 3] = cmk(v.x, v.y);
-  }
-  row2_from_01(m);
-}
-
-// One half-sweep of parity `parity` for all active copies (or_halfsweep_kernel per copy)
+// One half-sweep of parity `parity` for all active copies (or_halfsweep_kernel per
+// copy).  Work items run copy-minor: the ncopies blocks of one site block are adjacent
+// in the grid, so they run at about the same time and the site block's links (8 per
+// site) come from L2 for all but the first copy; each link crosses HBM about once per
+// half-sweep whatever the number of copies.
 template <typename T, int NDIR>
 __global__ void __launch_bounds__(kBatchBlock) or_batch_kernel(BDesc d, int parity, T omega) {
   typedef typename VecOf<T>::type V;
   constexpr int NC = Field<T, 12>::NCHUNK;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  V* sl = reinterpret_cast<V*>(smem_raw);  // [8 links][NC][block]
   const int ci = conf_of(d, blockIdx.x, &BConf::item_base);
   const BConf& C = d.c[ci];
   const int local = blockIdx.x - C.item_base;
-  const int grp = local / C.nblk, blk = local - grp * C.nblk;
-  const int tid = threadIdx.x;
-  const int i = blk * kBatchBlock + tid;
+  const int blk = local / C.ncopies, copy = local - blk * C.ncopies;
+  if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  const int i = blk * kBatchBlock + threadIdx.x;
   if (i >= C.L.vh) return;
   const size_t vh = (size_t)C.L.vh;
-  const int q = 1 - parity;
   const Site s = site_of(C.L, i, parity);
   const V* U = (const V*)(sizeof(T) == 4 ? C.U32 : C.U64);
-  // every thread stages its own site's links; no other thread reads them
-#pragma unroll
-  for (int mu = 0; mu < NDIR; mu++) {
-    const V* Uf = U + (size_t)(parity * 4 + mu) * NC * vh;
-    const V* Ub = U + (size_t)(q * 4 + mu) * NC * vh;
-    const int jb = nb_bwd(C.L, s, mu);
-#pragma unroll
-    for (int c = 0; c < NC; c++) {
-      sl[(mu * NC + c) * kBatchBlock + tid] = __ldg(Uf + c * vh + i);
-      sl[((4 + mu) * NC + c) * kBatchBlock + tid] = __ldg(Ub + c * vh + jb);
-    }
-  }
-  V* G0 = (V*)(sizeof(T) == 4 ? C.G32 : C.G64);
-  const size_t gstride = sizeof(T) == 4 ? C.gstride32 : C.gstride64;
-#pragma unroll 1
-  for (int k = 0; k < d.K; k++) {
-    const int copy = grp * d.K + k;
-    if (copy >= C.ncopies) break;
-    if (d.states[C.copy_base + copy].done != 0) continue;
-    V* G = G0 + (size_t)copy * gstride;
-    const V* Gq = G + (size_t)q * NC * vh;
-    Mat3<T> star;
-    mzero(star);
-#pragma unroll
-    for (int mu = 0; mu < NDIR; mu++) {
-      Mat3<T> a, b;
-      smem_load12<T>(sl, mu, tid, a);
-      Field<T, 12>::load(Gq, vh, nb_fwd(C.L, s, mu), b);
-      addmul_nd(star, a, b);
-      const int jb = nb_bwd(C.L, s, mu);
-      smem_load12<T>(sl, 4 + mu, tid, a);
-      Field<T, 12>::load(Gq, vh, jb, b);
-      addmul_dd(star, a, b);
-    }
-    V* Gp = G + (size_t)parity * NC * vh;
-    Mat3<T> gold, g, gn;
-    Field<T, 12>::load(Gp, vh, i, gold);
-    g = gold;
-    cm_relax(g, star);
-    normalize<T, true>(g);
-    overrelax_rows01(gn, gold, g, omega);
-    Field<T, 12>::store(Gp, vh, i, gn);
-  }
+  V* G = (V*)(sizeof(T) == 4 ? C.G32 : C.G64) +
+         (size_t)copy * (sizeof(T) == 4 ? C.gstride32 : C.gstride64);
+  Mat3<T> star;
+  compute_star<T, T, 12, T, 12, NDIR>(C.L, s, parity, U, G, star);
+  V* Gp = G + (size_t)parity * NC * vh;
+  Mat3<T> gold, g, gn;
+  Field<T, 12>::load(Gp, vh, i, gold);
+  g = gold;
+  cm_relax(g, star);
+  normalize<T, true>(g);
+  overrelax_rows01(gn, gold, g, omega);
+  Field<T, 12>::store(Gp, vh, i, gn);
 }
 
 // Per-copy functional partials (measure_kernel per copy, same block grouping)
@@ -274,7 +214,6 @@ struct gfx_batch {
   int nconf;
   int ncopies;
   int precision;
-  int K;
   cudaStream_t stream;
   bool own_stream;
   std::vector<std::array<int, 4>> dims;
@@ -322,10 +261,8 @@ gfx_status balloc(gfx_batch* b, void** p, size_t bytes) {
   return GFX_OK;
 }
 
-size_t smem_bytes(int prec) { return (size_t)8 * (prec == 0 ? 3 : 6) * kBatchBlock * 16; }
-
 void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
-  const size_t sm = smem_bytes(prec);
+  const size_t sm = 0;
   for (int p = 0; p < 2; p++) {
     if (prec == 0) {
       if (ndir == 4)
@@ -446,7 +383,7 @@ gfx_status gfx_batch_destroy(gfx_batch* b) {
 }
 
 gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const int* ncopies,
-                            int precision, int copies_per_item, void* stream) {
+                            int precision, void* stream) {
   gfx_batch* b = nullptr;
   if (!out || !dims || !ncopies) return bfail(nullptr, GFX_ERR_ARG, "gfx_batch_create: NULL argument");
   *out = nullptr;
@@ -464,7 +401,6 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
   b = new gfx_batch();
   b->nconf = nconf;
   b->precision = precision;
-  b->K = copies_per_item > 0 ? copies_per_item : 8;
   b->running = nullptr;
   b->h_states = nullptr;
   std::memset((void*)&b->desc, 0, sizeof(b->desc));
@@ -500,7 +436,6 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     C.ncopies = ncopies[c];
     C.copy_base = copy_base;
     C.nblk = (C.L.vh + kBatchBlock - 1) / kBatchBlock;
-    C.ngroups = (C.ncopies + b->K - 1) / b->K;
     C.item_base = item;
     C.nbx = (C.L.st + kBatchBlock - 1) / kBatchBlock;
     C.mitem_base = mitem;
@@ -522,7 +457,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
       C.G32 = p;
     }
     copy_base += C.ncopies;
-    item += C.nblk * C.ngroups;
+    item += C.nblk * C.ncopies;
     mitem += C.ncopies * 2 * C.L.lt * C.nbx;
     sitem += C.ncopies * C.L.lt;
     slice += C.ncopies * C.L.lt;
@@ -534,7 +469,6 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
   b->nsitems = sitem;
   b->desc.nconf = nconf;
   b->desc.ncopies = copy_base;
-  b->desc.K = b->K;
   void* p;
   BTRY(balloc(b, &p, sizeof(LoopState) * copy_base));
   b->desc.states = (LoopState*)p;
@@ -551,14 +485,6 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     return bfail(nullptr, GFX_ERR_OOM, "cudaMallocHost failed");
   }
   std::memset(b->h_states, 0, sizeof(LoopState) * copy_base);
-  if (cudaFuncSetAttribute(or_batch_kernel<double, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem_bytes(1)) != cudaSuccess ||
-      cudaFuncSetAttribute(or_batch_kernel<double, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem_bytes(1)) != cudaSuccess) {
-    cudaGetLastError();
-    gfx_batch_destroy(b);
-    return bfail(nullptr, GFX_ERR_CUDA, "cannot raise the shared-memory limit of the sweep kernel");
-  }
 #undef BTRY
   *out = b;
   return GFX_OK;

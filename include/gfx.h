@@ -229,10 +229,9 @@ typedef struct {
 } gfx_copy_result;
 
 /* nconf configurations with extents dims[4*c..4*c+3] and ncopies[c] gauge copies each
- * (at most 8 configurations); copies_per_item = copies updated per staged set of links
- * (0: 8) */
+ * (at most 8 configurations) */
 gfx_status gfx_batch_create(gfx_batch **out, int nconf, const int *dims, const int *ncopies,
-                            int precision, int copies_per_item, void *stream);
+                            int precision, void *stream);
 gfx_status gfx_batch_destroy(gfx_batch *b);
 const char *gfx_batch_last_error(const gfx_batch *b);
 int gfx_batch_copies(const gfx_batch *b);

@@ -11,8 +11,8 @@ pytestmark = pytest.mark.gpu
 DIMS = [(8, 8, 8, 8), (4, 6, 8, 10)]
 
 
-def _batch(gfx, prec, ncopies, K, seed=900):
-    b = gfx.Batch(DIMS, ncopies, precision=prec, copies_per_item=K)
+def _batch(gfx, prec, ncopies, seed=900):
+    b = gfx.Batch(DIMS, ncopies, precision=prec)
     links = [smooth_links(d, 0.3 + 0.1 * c, 50 + c) for c, d in enumerate(DIMS)]
     for c, u in enumerate(links):
         b.set_links(c, u)
@@ -20,10 +20,9 @@ def _batch(gfx, prec, ncopies, K, seed=900):
     return b, links
 
 
-@pytest.mark.parametrize("prec,K", [(2, 8), (2, 2), (0, 3)])
-def test_batch_copies_match_single_contexts(gfx, prec, K):
-    ncopies = [5, 3]
-    b, links = _batch(gfx, prec, ncopies, K)
+@pytest.mark.parametrize("prec,ncopies", [(2, [5, 3]), (2, [1, 7]), (0, [3, 2])])
+def test_batch_copies_match_single_contexts(gfx, prec, ncopies):
+    b, links = _batch(gfx, prec, ncopies)
     kw = dict(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA,
               switch_eps=1e-9, checkinterval_double=5)
     res, ms = b.overrelax(**kw)
@@ -48,7 +47,7 @@ def test_batch_copies_match_single_contexts(gfx, prec, K):
 
 
 def test_batch_best_copy(gfx):
-    b, links = _batch(gfx, 2, [6, 2], 4)
+    b, links = _batch(gfx, 2, [6, 2])
     res, _ = b.overrelax(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7,
                          criterion=gfx.CRIT_THETA)
     k, f = b.best(0)
