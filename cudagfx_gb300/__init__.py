@@ -1,8 +1,9 @@
 """cudagfx_gb300 -- Python host mirror of the cudagfx gauge-fixing interface on GB300.
 
 Everything here calls libgfx.so (the sm_103a CUDA library, C ABI in include/gfx.h)
-through ctypes.  There is no CPU fallback: importing the package raises when the
-library has not been built (``cudagfx_gb300.build.build()``).
+through ctypes.  There is no CPU fallback: importing the package builds the
+library when it is missing or stale (``cudagfx_gb300.build.build()``) and raises
+when that fails.
 
 Two layers, as in the C ABI:
   * ``Context``: one lattice on the GPU with explicit-argument methods
@@ -41,16 +42,17 @@ def library_path():
     return _LIB_PATH
 
 
-if not os.path.exists(_LIB_PATH):
-    # a fresh checkout: compile the library (nvcc, sm_103a); no fallback if that fails
-    try:
-        from . import build as _build
-        _build.build()
-    except Exception as e:  # noqa: BLE001
+# compile the library when it is missing or older than its sources (nvcc, sm_103a;
+# an mtime check when it is current).  No fallback: without the library, no import.
+try:
+    from . import build as _build
+    _build.build()
+except Exception as e:  # noqa: BLE001
+    if not os.path.exists(_LIB_PATH):
         raise ImportError("cudagfx_gb300: %s is missing and could not be built: %s"
                           % (_LIB_PATH, e)) from e
-    if not os.path.exists(_LIB_PATH):
-        raise ImportError("cudagfx_gb300: %s is missing" % _LIB_PATH)
+if not os.path.exists(_LIB_PATH):
+    raise ImportError("cudagfx_gb300: %s is missing" % _LIB_PATH)
 
 # RTLD_LOCAL: libgfx defines the reference's globals (LX, VOLUME, FUNC, ...); keep them
 # out of the global namespace so other libraries in the process keep their own.
@@ -101,6 +103,17 @@ class ThermParams(_c.Structure):
                 ("variant", _c.c_int)]
 
 
+class Tuning(_c.Structure):
+    _fields_ = [("block", _c.c_int * 2), ("staging", _c.c_int * 2), ("link_reals64", _c.c_int),
+                ("checkinterval", _c.c_int), ("sweep_ms", _c.c_double * 2),
+                ("check_ms", _c.c_double * 2)]
+
+    def as_dict(self):
+        return {"block": list(self.block), "staging": list(self.staging),
+                "link_reals64": self.link_reals64, "checkinterval": self.checkinterval,
+                "sweep_ms": list(self.sweep_ms), "check_ms": list(self.check_ms)}
+
+
 def _sig(name, res, args):
     f = getattr(lib, name)
     f.restype = res
@@ -119,6 +132,9 @@ _sig("gfx_destroy", _I, [_V])
 _sig("gfx_synchronize", _I, [_V])
 _sig("gfx_device_bytes", _c.c_size_t, [_V])
 _sig("gfx_set_block", _I, [_V, _I])
+_sig("gfx_get_tuning", _I, [_V, _c.POINTER(Tuning)])
+_sig("gfx_set_tuning", _I, [_V, _c.POINTER(Tuning)])
+_sig("gfx_autotune", _I, [_V, _I, _I, _c.c_char_p, _c.POINTER(Tuning)])
 for _n in ("gfx_set_links", "gfx_get_links", "gfx_set_trafo", "gfx_get_trafo"):
     _sig(_n, _I, [_V, _dp])
 _sig("gfx_unit_trafo", _I, [_V])
@@ -269,6 +285,28 @@ class Context:
 
     def set_block(self, b):
         self._check(lib.gfx_set_block(self._h, b))
+
+    def tuning(self):
+        t = Tuning()
+        self._check(lib.gfx_get_tuning(self._h, _c.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0):
+        """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first."""
+        t = Tuning()
+        t.block[0], t.block[1] = block
+        t.staging[0], t.staging[1] = staging
+        t.link_reals64 = link_reals64
+        t.checkinterval = checkinterval
+        self._check(lib.gfx_set_tuning(self._h, _c.byref(t)))
+
+    def autotune(self, gauge=LANDAU, expected_sweeps=0, cache_path=None):
+        """Time the candidate launch settings on this lattice and keep the fastest
+        (gfx_autotune); returns the chosen settings and their timings."""
+        t = Tuning()
+        self._check(lib.gfx_autotune(self._h, gauge, expected_sweeps,
+                                     cache_path.encode() if cache_path else None, _c.byref(t)))
+        return t.as_dict()
 
     def synchronize(self):
         self._check(lib.gfx_synchronize(self._h))

@@ -33,6 +33,76 @@ struct Load<double, float, 12> {
   }
 };
 
+// ---------------------------------------------------------------------------
+// L2 warm-up for one block of checkerboard sites [i0, i0 + n) of one parity.
+// In the even/odd SoA layout everything such a block reads lies in contiguous
+// ranges of 16-byte plane elements: its forward links and its own g at the block's
+// indices, and the other parity's g and backward links at the index shifts
+// 0/+-1 (x), +-sy, +-sz, +-st.  One cp.async.bulk.prefetch.L2 per range and plane,
+// issued by the first threads of the block before any load, puts all of the
+// block's DRAM requests in flight at once; the regular loads then hit L2.  It is a
+// hint: the neighbours that wrap around the lattice fall outside the ranges and
+// are fetched by the regular loads, and every range is clamped to its plane.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void l2_prefetch_range(const void* plane, int vh, int a, int b) {
+  a = max(a, 0);
+  b = min(b, vh);
+  if (b > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"((const char*)plane +
+                                                                     (size_t)a * 16),
+                 "r"((b - a) * 16)
+                 : "memory");
+}
+
+// NCU / NCG: 16-byte planes per link / per g.  U and G are the field bases.
+template <int NCU, int NCG, int NDIR>
+__device__ __forceinline__ void prefetch_range_k(const Lattice& L, int parity, int i0, int n,
+                                                 const void* U, const void* G, int k) {
+  constexpr int NSHIFT = 2 * NDIR - 1;  // x (both sides merged), then +-y, +-z, +-t
+  constexpr int N_FWD = NDIR * NCU, N_OWN = NCG, N_NB = NSHIFT * NCG;
+  const int vh = L.vh, q = 1 - parity;
+  const char* u = (const char*)U;
+  const char* g = (const char*)G;
+  const size_t plane = (size_t)vh * 16;
+  const int strides[4] = {0, L.sy, L.sz, L.st};
+  if (k < N_FWD) {
+    const int mu = k / NCU, c = k - mu * NCU;
+    l2_prefetch_range(u + ((size_t)(parity * 4 + mu) * NCU + c) * plane, vh, i0, i0 + n);
+    return;
+  }
+  k -= N_FWD;
+  if (k < N_OWN) {
+    l2_prefetch_range(g + ((size_t)parity * NCG + k) * plane, vh, i0, i0 + n);
+    return;
+  }
+  k -= N_OWN;
+  if (k < N_NB) {
+    const int r = k / NCG, c = k - r * NCG;
+    const char* p = g + ((size_t)q * NCG + c) * plane;
+    if (r == 0) {
+      l2_prefetch_range(p, vh, i0 - 1, i0 + n + 1);
+    } else {
+      const int s = strides[(r + 1) >> 1] * ((r & 1) ? 1 : -1);
+      l2_prefetch_range(p, vh, i0 + s, i0 + n + s);
+    }
+    return;
+  }
+  k -= N_NB;
+  const int mu = k / NCU, c = k - mu * NCU;
+  const int s = strides[mu];
+  l2_prefetch_range(u + ((size_t)(q * 4 + mu) * NCU + c) * plane, vh, i0 - s - (mu == 0),
+                    i0 + n - s);
+}
+
+template <int NCU, int NCG, int NDIR>
+__device__ __forceinline__ void prefetch_block(const Lattice& L, int parity, int i0, int n,
+                                               const void* U, const void* G) {
+  constexpr int NTOT = 2 * NDIR * NCU + 2 * NDIR * NCG;  // fwd + own + neighbours + bwd
+  for (int k = threadIdx.x; k < NTOT; k += blockDim.x)
+    prefetch_range_k<NCU, NCG, NDIR>(L, parity, i0, n, U, G, k);
+}
+
+
 // star w(x) = sum_mu U_mu(x) g^+(x+mu) + U_mu^+(x-mu) g^+(x-mu)   (overrelax.cu:350-394)
 template <typename TC, typename TSU, int NRU, typename TSG, int NRG, int NDIR>
 __device__ __forceinline__ void compute_star(const Lattice& L, const Site& c, int parity,

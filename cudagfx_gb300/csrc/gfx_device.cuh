@@ -369,12 +369,8 @@ __device__ __forceinline__ T* mat_scalar(Mat3<T>& m, int k) {
 __device__ __forceinline__ float4 ldg_stream(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ double2 ldg_stream(const double2* p) { return __ldg(p); }
 
-template <>
-__device__ __forceinline__ void Field<float, 12>::load(const float4* __restrict__ base,
-                                                       size_t stride, int i, Mat3<float>& m) {
-  float4 a = __ldg(base + i);
-  float4 b = __ldg(base + stride + i);
-  float4 c = __ldg(base + 2 * stride + i);
+// rows 0,1 from the three 16-byte chunks of an FP32 12-real matrix; row 2 rebuilt
+__device__ __forceinline__ void unpack12(float4 a, float4 b, float4 c, Mat3<float>& m) {
   m.e[0][0] = cmk(a.x, a.y);
   m.e[0][1] = cmk(a.z, a.w);
   m.e[0][2] = cmk(b.x, b.y);
@@ -383,6 +379,14 @@ __device__ __forceinline__ void Field<float, 12>::load(const float4* __restrict_
   m.e[1][2] = cmk(c.z, c.w);
   row2_from_01(m);
 }
+
+template <>
+__device__ __forceinline__ void Field<float, 12>::load(const float4* __restrict__ base,
+                                                       size_t stride, int i, Mat3<float>& m) {
+  unpack12(__ldg(base + i), __ldg(base + stride + i), __ldg(base + 2 * stride + i), m);
+}
+
+
 template <>
 __device__ __forceinline__ void Field<float, 12>::store(float4* __restrict__ base, size_t stride,
                                                         int i, const Mat3<float>& m) {

@@ -42,8 +42,9 @@ struct Reduced {
 
 // ----- kernel launchers (gfx_kernels.cu) -----
 // precision tags: 0 = FP32 12-real, 1 = FP64 12-real, 2 = FP64 18-real (links only)
+// mode: 0 plain loads, 1 L2 bulk prefetch per block
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
-                         int parity, double omega, int block, cudaStream_t s);
+                         int parity, double omega, int block, int mode, cudaStream_t s);
 // measure: compute precision (0 float, 1 double), g storage (0 float, 1 double)
 void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
                     const void* G, double* partials, int block, cudaStream_t s);

@@ -2,6 +2,8 @@
 // plaquette, Polyakov loop and field-layout kernels for sm_103a.
 #include <cstdio>
 
+#include <algorithm>
+
 #include "gfx_common.cuh"
 #include "gfx_internal.h"
 
@@ -37,14 +39,21 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // ---------------------------------------------------------------------------
 // overrelaxation half-sweep (overrelax.cu:335-446), in place on parity `parity`
 // ---------------------------------------------------------------------------
-template <typename T, int NRU, int NDIR>
+// MODE (launch_or_halfsweep's mode): 0 plain loads; 1 each block first issues one
+// L2 bulk prefetch per contiguous range it reads.
+template <typename T, int NRU, int NDIR, int MODE>
 __global__ void __launch_bounds__(256) or_halfsweep_kernel(Lattice L,
                                                             const typename VecOf<T>::type* U,
                                                             typename VecOf<T>::type* G, int parity,
                                                             T omega) {
+  constexpr int NCG = Field<T, 12>::NCHUNK;
+  constexpr int NCU = Field<T, NRU>::NCHUNK;
+  if (MODE == 1) {
+    const int i0 = blockIdx.x * blockDim.x;
+    prefetch_block<NCU, NCG, NDIR>(L, parity, i0, min((int)blockDim.x, L.vh - i0), U, G);
+  }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= L.vh) return;
-  constexpr int NCG = Field<T, 12>::NCHUNK;
   const size_t vh = (size_t)L.vh;
   const Site c = site_of(L, i, parity);
   Mat3<T> star;
@@ -60,11 +69,17 @@ __global__ void __launch_bounds__(256) or_halfsweep_kernel(Lattice L,
 }
 
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
-                         int parity, double omega, int block, cudaStream_t s) {
-  dim3 grid((L.vh + block - 1) / block);
-#define OR_LAUNCH(T, NR, ND)                                                                    \
-  or_halfsweep_kernel<T, NR, ND><<<grid, block, 0, s>>>(                                     \
-      L, (const typename VecOf<T>::type*)U, (typename VecOf<T>::type*)G, parity, (T)omega)
+                         int parity, double omega, int block, int mode, cudaStream_t s) {
+  const dim3 grid((L.vh + block - 1) / block);
+#define OR_LAUNCH(T, NR, ND)                                                                     \
+  do {                                                                                           \
+    const auto* u_ = (const typename VecOf<T>::type*)U;                                          \
+    auto* g_ = (typename VecOf<T>::type*)G;                                                      \
+    if (mode == 1)                                                                               \
+      or_halfsweep_kernel<T, NR, ND, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
+    else                                                                                         \
+      or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
+  } while (0)
   if (prec == 0) {
     if (ndir == 4) OR_LAUNCH(float, 12, 4);
     else OR_LAUNCH(float, 12, 3);

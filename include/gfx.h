@@ -131,6 +131,42 @@ size_t gfx_device_bytes(const gfx_ctx *ctx);
 /* threads per block of the sweep kernels (0: library default / autotuned) */
 gfx_status gfx_set_block(gfx_ctx *ctx, int block);
 
+/* ---- launch tuning (no reference counterpart: the reference hard-codes 128
+ *      threads per block, cudaglobal.h:8) ----
+ * Settings of the overrelaxation half-sweep per precision, [0] = FP32 storage,
+ * [1] = FP64.  block: threads per block (a multiple of 32 in [32, 256]).
+ * staging: 0 = plain 128-bit loads; 1 = each block first issues one L2 bulk
+ * prefetch (cp.async.bulk.prefetch.L2) per contiguous range it reads.  All
+ * settings give bit-identical results.
+ * link_reals64: FP64 link storage, 12 (two rows) or 18 (full).
+ * checkinterval: sweeps per convergence check the tuner suggests for the FP32
+ * phase (0 = no suggestion).  sweep_ms / check_ms: the tuner's timings of one full
+ * sweep and of one check at the chosen settings (0 when set by hand). */
+typedef struct {
+  int block[2];
+  int staging[2];
+  int link_reals64;
+  int checkinterval;
+  double sweep_ms[2];
+  double check_ms[2];
+} gfx_tuning;
+
+gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
+/* Apply settings (block, staging, link_reals64; the timings are ignored).  A
+ * change of link_reals64 re-packs the FP64 links on the device. */
+gfx_status gfx_set_tuning(gfx_ctx *ctx, const gfx_tuning *t);
+/* Time every candidate setting on this context's lattice and apply the fastest.
+ * Candidates: block 64/128/192/256 x staging 0/1 for each precision the
+ * context holds, and for FP64 both link layouts.  The fields are left as they
+ * were: the candidate sweeps run on g and it is restored afterwards.
+ * expected_sweeps > 0 also sets checkinterval to the interval that minimises
+ * check time plus the sweeps run past convergence, sqrt(2 n check_ms / sweep_ms),
+ * clamped to [5, 100].  cache_path (or NULL): a text file of earlier results keyed
+ * by device, lattice, precision mode and gauge; a hit applies the stored settings
+ * without timing, a miss appends the new result. */
+gfx_status gfx_autotune(gfx_ctx *ctx, int gauge, int expected_sweeps, const char *cache_path,
+                        gfx_tuning *out);
+
 /* ---- fields (init_gaugefixing / gfx_get_trafo of the reference's main, cudagaugefix.cu:204-374, 785-793) ---- */
 gfx_status gfx_set_links(gfx_ctx *ctx, const double *su3_links);
 gfx_status gfx_get_links(gfx_ctx *ctx, double *su3_links);

@@ -1,0 +1,83 @@
+"""Launch tuning: every block size, both staging modes (plain loads, L2 bulk prefetch)
+and both FP64 link layouts give bit-identical sweeps; gfx_autotune leaves the fields as it found them, its
+choice reproduces the untuned solve exactly, and its cache file round-trips."""
+import numpy as np
+import pytest
+
+import cudagfx_gb300 as gfx
+
+pytestmark = pytest.mark.gpu
+
+DIMS = (8, 8, 8, 12)
+V = int(np.prod(DIMS))
+
+
+def _ctx(prec=gfx.PREC_MIXED):
+    c = gfx.Context(DIMS, precision=prec)
+    c.set_links(gfx.random_init_haar(5, 4 * V))
+    c.set_trafo(gfx.random_init_reference(351, V))
+    return c
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_launch_variants_are_bit_identical(prec):
+    ref = _ctx()
+    ref.or_sweeps(3, omega=1.7, precision=prec)
+    want = ref.get_trafo()
+    ref.close()
+    for nr in ((12, 18) if prec == 1 else (12,)):
+        for block in (32, 64, 96, 128, 192, 256):
+            for pf in (0, 1):
+                c = _ctx()
+                c.set_tuning(block=(block, block), staging=(pf, pf), link_reals64=nr)
+                c.or_sweeps(3, omega=1.7, precision=prec)
+                assert np.array_equal(c.get_trafo(), want), (nr, block, pf)
+                c.close()
+
+
+def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
+    kw = dict(maxit=3000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA)
+    a = _ctx()
+    g0 = a.get_trafo()
+    u0 = a.get_links()
+    ra = a.overrelax(**kw)
+    ga = a.get_trafo()
+    b = _ctx()
+    t = b.autotune(expected_sweeps=1000, cache_path=str(tmp_path / "tune.txt"))
+    assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1)
+    assert t["link_reals64"] in (12, 18) and 5 <= t["checkinterval"] <= 100
+    assert t["sweep_ms"][0] > 0 and t["check_ms"][1] > 0
+    assert np.array_equal(b.get_trafo(), g0)
+    assert np.max(np.abs(b.get_links() - u0)) < 1e-15
+    rb = b.overrelax(**kw)
+    assert (rb.iterations, rb.sweeps_single, rb.sweeps_double) == \
+        (ra.iterations, ra.sweeps_single, ra.sweeps_double)
+    assert rb.final_values.F == ra.final_values.F
+    assert np.array_equal(b.get_trafo(), ga)
+    a.close()
+    b.close()
+
+
+def test_autotune_cache_hit_applies_stored_settings(tmp_path):
+    path = str(tmp_path / "tune.txt")
+    a = _ctx()
+    t1 = a.autotune(cache_path=path)
+    a.close()
+    lines = open(path).read().splitlines()
+    assert len(lines) == 1 and "8x8x8x12" in lines[0]
+    b = _ctx()
+    t2 = b.autotune(cache_path=path)
+    assert (t2["block"], t2["staging"], t2["link_reals64"]) == \
+        (t1["block"], t1["staging"], t1["link_reals64"])
+    assert b.tuning()["block"] == t1["block"]
+    assert len(open(path).read().splitlines()) == 1  # a hit appends nothing
+    b.close()
+
+
+def test_set_tuning_rejects_bad_settings():
+    c = _ctx()
+    for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(2, 0)), dict(staging=(0, -1)),
+                dict(link_reals64=8)):
+        with pytest.raises(gfx.GfxError):
+            c.set_tuning(**bad)
+    c.close()
