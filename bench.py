@@ -55,10 +55,14 @@ def parse():
     ap.add_argument("--beta", type=float, default=6.0)
     ap.add_argument("--eps", type=float, default=1e-12)
     ap.add_argument("--omega", type=float, default=1.7)
-    ap.add_argument("--checkinterval", type=int, default=25)
+    ap.add_argument("--checkinterval", type=int, default=0,
+                    help="sweeps per check (0: the autotuner's choice)")
     ap.add_argument("--switch-eps", type=float, default=1e-10)
-    ap.add_argument("--checkinterval-double", type=int, default=5)
+    ap.add_argument("--checkinterval-double", type=int, default=2)
+    ap.add_argument("--checkinterval-near", type=int, default=10,
+                    help="sweeps per check once theta < switch-eps (0: off)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
+    ap.add_argument("--no-tune", action="store_true", help="library default launch settings")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven check loop instead of the CUDA-graph while loop (same "
                          "kernels; profilers list each launch)")
@@ -81,7 +85,7 @@ def gribov_batch(args, gfx, mt_source):
     single-lattice solve per copy.  Both timed with CUDA events (solve only)."""
     confs = [((16, 16, 16, 16), 6.0), ((24, 24, 24, 24), 6.2)]
     ncopies = [int(x) for x in args.gribov_copies.split(",")]
-    kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval, omega=args.omega,
+    kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval or 25, omega=args.omega,
               criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
               checkinterval_double=args.checkinterval_double)
     links = []
@@ -357,26 +361,37 @@ def run_gfx(args, dims):
     plaq = ctx.plaquette()
     links = ctx.get_links()
     g0 = gfx.random_init_reference(351 + rank, V)
-    params = ctx.or_params(maxit=20000, eps=args.eps, checkinterval=args.checkinterval,
-                           omega=args.omega, criterion=gfx.CRIT_THETA,
-                           switch_eps=args.switch_eps,
-                           checkinterval_double=args.checkinterval_double,
-                           use_graph=0 if args.no_graph else 1)
 
-    def solve(c):
+    def make_params(ck):
+        return ctx.or_params(maxit=20000, eps=args.eps, checkinterval=ck, omega=args.omega,
+                             criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
+                             checkinterval_double=args.checkinterval_double,
+                             checkinterval_near=args.checkinterval_near,
+                             use_graph=0 if args.no_graph else 1)
+
+    def solve(c, p):
         c.set_trafo(g0)
-        r = c.overrelax(params)
+        r = c.overrelax(p)
         if not r.converged:
             raise RuntimeError("did not converge: %d sweeps" % r.sweeps)
         return r
 
+    # ---- launch tuning (before any timing): the first warm-up solve gives the sweep
+    # count the check interval is chosen for
+    params = make_params(args.checkinterval or 25)
+    r_w = solve(ctx, params)
+    tune = None
+    if not args.no_tune:
+        tune = ctx.autotune(gfx.LANDAU, expected_sweeps=r_w.sweeps_single)
+    if args.checkinterval == 0 and tune:
+        params = make_params(tune["checkinterval"])
     for _ in range(args.warmup):
-        solve(ctx)
+        solve(ctx, params)
     # ---- timed region: K solves, device time of each (CUDA events on the ctx stream)
     barrier(dist)
     launches0 = ctx.launch_count()
     with ClockSampler(local) as clk:
-        results = [solve(ctx) for _ in range(args.steps)]
+        results = [solve(ctx, params) for _ in range(args.steps)]
     launches = ctx.launch_count() - launches0
     ms_total = sum(r.ms for r in results)
     ms_total = max_over_ranks(dist, ms_total)
@@ -411,12 +426,19 @@ def run_gfx(args, dims):
     ms64 = None
     t_fp64 = None
     sweeps64 = None
+    tune64 = None
     if not args.no_fp64:
         c64 = gfx.Context(dims, precision=gfx.PREC_DOUBLE)
         c64.set_links(links)
         c64.set_trafo(g0)
+        p64 = params
+        if not args.no_tune:
+            # the all-FP64 run gets its own tuning (FP64 link layout, check interval)
+            tune64 = c64.autotune(gfx.LANDAU, expected_sweeps=r_last.sweeps)
+            if args.checkinterval == 0:
+                p64 = make_params(tune64["checkinterval"])
         ms64 = c64.time_sweeps(4, args.omega, precision=1) / 8
-        r64 = solve(c64)
+        r64 = solve(c64, p64)
         t_fp64 = r64.ms / 1000.0
         sweeps64 = r64.sweeps
         c64.close()
@@ -459,7 +481,11 @@ def run_gfx(args, dims):
                         "OR omega=%g to theta<%g" % ("x".join(map(str, dims)), args.beta,
                                                      args.therm, args.omega, args.eps),
             "lattice": list(dims), "omega": args.omega, "eps": args.eps, "criterion": "theta",
-            "checkinterval": args.checkinterval, "parallelism": "replicas" if ws > 1 else "1 GPU",
+            "checkinterval": params.checkinterval,
+            "checkinterval_double": params.checkinterval_double,
+            "checkinterval_near": params.checkinterval_near,
+            "tuning": tune, "tuning_fp64": tune64,
+            "parallelism": "replicas" if ws > 1 else "1 GPU",
             "l2": "inputs larger than L2 (FP32 links %d MB, FP64 links %d MB)"
                   % (V * 4 * 48 // 2 ** 20, V * 4 * 96 // 2 ** 20),
             "mt_params": "reference file" if dat else "synthetic stand-in",

@@ -78,7 +78,7 @@ class ORParams(_c.Structure):
                 ("omega", _c.c_double), ("criterion", _c.c_int), ("gauge", _c.c_int),
                 ("switch_eps", _c.c_double), ("plateau_ratio", _c.c_double),
                 ("checkinterval_double", _c.c_int), ("use_graph", _c.c_int),
-                ("record_history", _c.c_int)]
+                ("record_history", _c.c_int), ("checkinterval_near", _c.c_int)]
 
 
 class ORResult(_c.Structure):

@@ -522,8 +522,8 @@ void gfx_or_params_default(gfx_or_params* p) {
   p->criterion = GFX_CRIT_MAXDADA;
   p->gauge = GFX_GAUGE_LANDAU;
   p->switch_eps = 1e-10;
-  p->plateau_ratio = 0.95;
-  p->checkinterval_double = 5;
+  p->plateau_ratio = 0.998;
+  p->checkinterval_double = 2;
   p->use_graph = 1;
   p->record_history = 1;
 }
@@ -601,7 +601,10 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   const bool handover = ctx->precision == GFX_PREC_MIXED;
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
-  const int hist_need = p.maxit / std::min(p.checkinterval, p.checkinterval_double) + 8;
+  if (p.checkinterval_near < 0) return fail(ctx, GFX_ERR_ARG, "checkinterval_near must be >= 0");
+  const int ck_min = std::min(std::min(p.checkinterval, p.checkinterval_double),
+                              p.checkinterval_near > 0 ? p.checkinterval_near : p.checkinterval);
+  const int hist_need = p.maxit / ck_min + 8;
   s = ensure_hist(ctx, hist_need);
   if (s) return s;
 
@@ -616,13 +619,18 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   // checkinterval_double applies to the FP64 polish after a mixed-precision handover;
   // a single-precision-mode run checks every checkinterval sweeps (overrelax.cu:775)
   H.ck = p.checkinterval;
+  H.ck_near = p.checkinterval_near;
   H.maxit = p.maxit;
   H.criterion = p.criterion;
   H.phase = handover ? 0 : 1;
   H.hist_cap = ctx->hist_cap;
   H.eps = p.eps;
   H.switch_eps = p.switch_eps;
-  H.plateau_ratio = p.plateau_ratio > 0 ? p.plateau_ratio : 1e300;
+  // plateau_ratio is per sweep: the threshold between checks k sweeps apart is ratio^k
+  H.plateau_ratio = p.plateau_ratio > 0 ? std::pow(p.plateau_ratio, p.checkinterval) : 1e300;
+  H.plateau_near = p.plateau_ratio > 0 && p.checkinterval_near > 0
+                       ? std::pow(p.plateau_ratio, p.checkinterval_near)
+                       : H.plateau_ratio;
   s = write_loop(ctx);
   if (s) return s;
 
@@ -659,6 +667,14 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       }
       (prec == 0 ? sweeps_single : sweeps_double) += H.iter - it0;
     }
+    if (H.done == 4) {
+      // below switch_eps: the same phase continues with the shorter interval
+      H.ck = H.ck_near;
+      H.done = 0;
+      s = write_loop(ctx);
+      if (s) return s;
+      continue;
+    }
     if (H.done == 2) {
       // FP32 phase finished: widen g (reunitarized in FP64) and verify in FP64
       s = prepare_g(ctx, 1);
@@ -668,6 +684,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       H.done = 0;
       H.prev = 0.0;
       H.ck = p.checkinterval_double;
+      H.ck_near = 0;
       s = write_loop(ctx);
       if (s) return s;
       enqueue_measure(ctx, 1, 1, ndir);

@@ -12,6 +12,7 @@
 // single-lattice kernels (gfx_common.cuh), so a copy's trajectory, iteration count and
 // final functional equal those of the same start fixed alone.
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <cstring>
 #include <string>
@@ -578,7 +579,7 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
     H.phase = handover ? 0 : 1;
     H.eps = p.eps;
     H.switch_eps = p.switch_eps;
-    H.plateau_ratio = p.plateau_ratio > 0 ? p.plateau_ratio : 1e300;
+    H.plateau_ratio = p.plateau_ratio > 0 ? std::pow(p.plateau_ratio, p.checkinterval) : 1e300;
   }
   gfx_status s = write_states(b);
   if (s) return s;

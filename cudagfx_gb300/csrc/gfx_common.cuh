@@ -258,12 +258,17 @@ __device__ __forceinline__ int reduce_and_check(const double* slice_sums, int lt
     // single-precision phase: hand over to the double-precision phase when the target
     // is reached (the FP64 phase verifies it), or when, below switch_eps, the value
     // stops decreasing -- the FP32 rounding floor, which a few FP64 sweeps remove
-    if (value < S.eps ||
-        (value < S.switch_eps && S.prev > 0.0 && value > S.plateau_ratio * S.prev))
+    // (the plateau threshold corresponds to the same decrease per sweep on either
+    // check interval)
+    const double plateau = S.ck_near > 0 && S.ck == S.ck_near ? S.plateau_near : S.plateau_ratio;
+    if (value < S.eps || (value < S.switch_eps && S.prev > 0.0 && value > plateau * S.prev))
       done = 2;
   } else if (value < S.eps) {
     done = 1;
   }
+  // close to the end: shorter intervals cut the sweeps run past convergence (or past
+  // the FP32 floor) while the long interval keeps the checks cheap before that
+  if (!done && S.ck_near > 0 && S.ck > S.ck_near && value < S.switch_eps) done = 4;
   if (!done && S.iter + S.ck >= S.maxit) done = 3;
   S.prev = value;
   S.done = done;

@@ -24,13 +24,16 @@ struct LoopState {
   int iter;       // iteration index of the last check
   int ck;         // sweeps between checks
   int maxit;      // iteration cap (exclusive, as in the reference loop)
-  int done;       // 0 running, 1 converged, 2 switch precision, 3 stopped at cap
+  int done;       // 0 running, 1 converged, 2 switch precision, 3 stopped at cap,
+                  // 4 below switch_eps: continue with ck_near sweeps between checks
+  int ck_near;    // sweeps between checks once the value is below switch_eps (0: ck)
   int criterion;  // GFX_CRIT_*
   int phase;
   int nhist, hist_cap;
   double eps;
   double switch_eps;     // phase 0 -> 1 when the monitored value drops below
-  double plateau_ratio;  // phase 0 -> 1 when value_new > ratio * value_old
+  double plateau_ratio;  // phase 0 -> 1 when value_new > plateau_ratio * value_old (ck sweeps apart)
+  double plateau_near;   // the same threshold for checks ck_near sweeps apart
   double prev;
   double last_F, last_dAdA, last_max, last_theta, last_theta_slice_max;
 };

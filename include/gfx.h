@@ -68,10 +68,13 @@ typedef struct {
   int criterion;          /* gfx_criterion */
   int gauge;              /* gfx_gauge */
   double switch_eps;      /* mixed: below this the FP32 phase ends when the value stalls */
-  double plateau_ratio;   /* mixed: stalled = value_new > plateau_ratio * value_old */
+  double plateau_ratio;   /* mixed: per sweep; stalled = value_new > plateau_ratio^k * value_old
+                             for checks k sweeps apart (default 0.998) */
   int checkinterval_double; /* sweeps between checks in the FP64 phase (0: checkinterval) */
   int use_graph;          /* 1: device-side loop in a CUDA graph (conditional while node) */
   int record_history;     /* keep every check (gfx_or_history) */
+  int checkinterval_near; /* sweeps between checks once the value is below switch_eps
+                             (0: checkinterval throughout, the reference schedule) */
 } gfx_or_params;
 
 typedef struct {

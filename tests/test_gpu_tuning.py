@@ -5,6 +5,7 @@ import numpy as np
 import pytest
 
 import cudagfx_gb300 as gfx
+from conftest import smooth_links
 
 pytestmark = pytest.mark.gpu
 
@@ -81,3 +82,29 @@ def test_set_tuning_rejects_bad_settings():
         with pytest.raises(gfx.GfxError):
             c.set_tuning(**bad)
     c.close()
+
+
+@pytest.mark.parametrize("prec", [gfx.PREC_DOUBLE, gfx.PREC_MIXED])
+def test_checkinterval_near_shortens_the_end(prec):
+    """Below switch_eps the loop continues with checkinterval_near sweeps per check:
+    the same sweeps up to that point, the shorter spacing after it, and convergence."""
+    kw = dict(maxit=4000, eps=1e-12, checkinterval=40, omega=1.7, criterion=gfx.CRIT_THETA,
+              switch_eps=1e-8)
+    links = smooth_links(DIMS, 0.4, 77)
+    a = _ctx(prec)
+    a.set_links(links)
+    ra = a.overrelax(**kw)
+    ha = a.history()
+    b = _ctx(prec)
+    b.set_links(links)
+    rb = b.overrelax(checkinterval_near=4, **kw)
+    hb = b.history()
+    assert ra.converged and rb.converged
+    assert rb.final_values.theta < 1e-12
+    first = next(k for k, h in enumerate(ha) if h["theta"] < 1e-8)
+    assert [h["iter"] for h in hb[:first + 1]] == [h["iter"] for h in ha[:first + 1]]
+    # the near interval, or the FP64 polish (its first check verifies at the same iteration)
+    assert hb[first + 1]["iter"] - hb[first]["iter"] in (0, 2, 4)
+    assert rb.sweeps <= ra.sweeps
+    a.close()
+    b.close()
