@@ -458,6 +458,25 @@ class Context:
     def link_heatbath_halfsweep(self, parity, nu, beta, variant=HB_REFERENCE):
         self._check(lib.gfx_link_heatbath_halfsweep(self._h, parity, nu, beta, variant))
 
+    # ---- files (include/gfx_io.h)
+    def load_links_ildg(self, path):
+        info = IldgInfo()
+        self._check(lib.gfx_load_links_ildg(self._h, os.fsencode(path), _c.byref(info)))
+        return info.as_dict()
+
+    def write_links_ildg(self, path, precision=64, beta=0.0):
+        self._check(lib.gfx_write_links_ildg(self._h, os.fsencode(path), precision, beta))
+
+    def write_fixed_ildg(self, path, precision=64, beta=0.0):
+        """The gauge-fixed field g U g^+ as an ILDG file; the context is unchanged."""
+        self._check(lib.gfx_write_fixed_ildg(self._h, os.fsencode(path), precision, beta))
+
+    def checkpoint_save(self, path):
+        self._check(lib.gfx_checkpoint_save(self._h, os.fsencode(path)))
+
+    def checkpoint_load(self, path):
+        self._check(lib.gfx_checkpoint_load(self._h, os.fsencode(path)))
+
 
 class CopyResult(_c.Structure):
     _fields_ = [("conf", _c.c_int), ("copy", _c.c_int), ("converged", _c.c_int),
@@ -553,3 +572,135 @@ def sa_temperature(Tmin, Tmax, N, expo, i):
 
 
 from . import legacy  # noqa: E402,F401  (reference-named entry points)
+
+
+# ---------------------------------------------------------------------------
+# gauge-field files (include/gfx_io.h): ILDG, BQCD, POSIX cksum
+# ---------------------------------------------------------------------------
+class IldgInfo(_c.Structure):
+    _fields_ = [("dims", _I * 4), ("precision", _I), ("plaquette", _c.c_double),
+                ("beta", _c.c_double), ("data_bytes", _c.c_uint64)]
+
+    def as_dict(self):
+        return {"dims": tuple(self.dims), "precision": self.precision,
+                "plaquette": self.plaquette, "beta": self.beta, "data_bytes": self.data_bytes}
+
+
+class SliceCksum(_c.Structure):
+    _fields_ = [("file", _c.c_char * 80), ("sum", _c.c_uint64), ("bytes", _c.c_uint64)]
+
+
+class BqcdInfo(_c.Structure):
+    _fields_ = [("run", _I), ("dims", _I * 4), ("beta", _c.c_double), ("plaquette", _c.c_double)]
+
+
+class CksumState(_c.Structure):
+    _fields_ = [("crc", _c.c_uint32), ("bytes", _c.c_uint64)]
+
+
+_sig("gfx_ildg_read_info", _I, [_c.c_char_p, _c.POINTER(IldgInfo)])
+_sig("gfx_ildg_read", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _c.POINTER(IldgInfo)])
+_sig("gfx_ildg_write", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _I, _D, _D])
+_sig("gfx_cksum_init", None, [_c.POINTER(CksumState)])
+_sig("gfx_cksum_add", None, [_c.POINTER(CksumState), _V, _c.c_size_t])
+_sig("gfx_cksum_get", _c.c_uint32, [_c.POINTER(CksumState)])
+_sig("gfx_bqcd_write", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _D, _D, _I,
+                            _c.POINTER(SliceCksum)])
+_sig("gfx_bqcd_read", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _c.POINTER(SliceCksum)])
+_sig("gfx_bqcd_read_trafo", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _c.POINTER(SliceCksum)])
+_sig("gfx_bqcd_write_trafo", _I, [_c.c_char_p, _c.POINTER(_I), _dp, _c.POINTER(SliceCksum)])
+_sig("gfx_bqcd_read_info", _I, [_c.c_char_p, _c.POINTER(BqcdInfo), _c.POINTER(SliceCksum), _I,
+                                _c.POINTER(_I)])
+_sig("gfx_load_links_ildg", _I, [_V, _c.c_char_p, _c.POINTER(IldgInfo)])
+_sig("gfx_write_links_ildg", _I, [_V, _c.c_char_p, _I, _D])
+_sig("gfx_write_fixed_ildg", _I, [_V, _c.c_char_p, _I, _D])
+_sig("gfx_checkpoint_save", _I, [_V, _c.c_char_p])
+_sig("gfx_checkpoint_load", _I, [_V, _c.c_char_p])
+
+
+def _io_check(s):
+    if s != 0:
+        raise GfxError(s, lib.gfx_last_error(None).decode())
+
+
+def _dims4(dims):
+    return (_I * 4)(*[int(x) for x in dims])
+
+
+def _cks_list(arr, n):
+    return [{"file": arr[k].file.decode(), "sum": arr[k].sum, "bytes": arr[k].bytes}
+            for k in range(n)]
+
+
+def ildg_read_info(path):
+    info = IldgInfo()
+    _io_check(lib.gfx_ildg_read_info(os.fsencode(path), _c.byref(info)))
+    return info.as_dict()
+
+
+def ildg_read(path, dims):
+    """links (4V, 3, 3, 2) and the file's metadata"""
+    V = int(np.prod(dims))
+    out = np.empty((4 * V, 3, 3, 2))
+    info = IldgInfo()
+    _io_check(lib.gfx_ildg_read(os.fsencode(path), _dims4(dims), _ptr(out), _c.byref(info)))
+    return out, info.as_dict()
+
+
+def ildg_write(path, dims, links, precision=64, plaquette=0.0, beta=0.0):
+    V = int(np.prod(dims))
+    a = _f64(links, 4 * V)
+    _io_check(lib.gfx_ildg_write(os.fsencode(path), _dims4(dims), _ptr(a), precision,
+                                 plaquette, beta))
+
+
+def cksum(data):
+    """POSIX cksum of a bytes-like object: (crc, byte count)"""
+    b = bytes(data)
+    st = CksumState()
+    lib.gfx_cksum_init(_c.byref(st))
+    buf = _c.create_string_buffer(b, len(b))
+    lib.gfx_cksum_add(_c.byref(st), _c.cast(buf, _V), len(b))
+    return int(lib.gfx_cksum_get(_c.byref(st))), int(st.bytes)
+
+
+def bqcd_write(basename, dims, links, plaquette=0.0, beta=0.0, ensemble=0):
+    V = int(np.prod(dims))
+    a = _f64(links, 4 * V)
+    cks = (SliceCksum * dims[3])()
+    _io_check(lib.gfx_bqcd_write(os.fsencode(basename), _dims4(dims), _ptr(a), plaquette, beta,
+                                 ensemble, cks))
+    return _cks_list(cks, dims[3])
+
+
+def bqcd_read(basename, dims):
+    V = int(np.prod(dims))
+    out = np.empty((4 * V, 3, 3, 2))
+    cks = (SliceCksum * dims[3])()
+    _io_check(lib.gfx_bqcd_read(os.fsencode(basename), _dims4(dims), _ptr(out), cks))
+    return out, _cks_list(cks, dims[3])
+
+
+def bqcd_write_trafo(basename, dims, trafo):
+    V = int(np.prod(dims))
+    a = _f64(trafo, V)
+    cks = (SliceCksum * dims[3])()
+    _io_check(lib.gfx_bqcd_write_trafo(os.fsencode(basename), _dims4(dims), _ptr(a), cks))
+    return _cks_list(cks, dims[3])
+
+
+def bqcd_read_trafo(basename, dims):
+    V = int(np.prod(dims))
+    out = np.empty((V, 3, 3, 2))
+    cks = (SliceCksum * dims[3])()
+    _io_check(lib.gfx_bqcd_read_trafo(os.fsencode(basename), _dims4(dims), _ptr(out), cks))
+    return out, _cks_list(cks, dims[3])
+
+
+def bqcd_read_info(path, cap=4096):
+    info = BqcdInfo()
+    cks = (SliceCksum * cap)()
+    n = _I()
+    _io_check(lib.gfx_bqcd_read_info(os.fsencode(path), _c.byref(info), cks, cap, _c.byref(n)))
+    return ({"run": info.run, "dims": tuple(info.dims), "beta": info.beta,
+             "plaquette": info.plaquette}, _cks_list(cks, n.value))

@@ -31,6 +31,8 @@ UNITS = {
     "gfx_batch.cu": [],
     "gfx_host.cpp": [],
     "gfx_legacy.cpp": [],
+    "gfx_lime.cpp": [],
+    "gfx_io.cpp": [],
 }
 
 

@@ -68,9 +68,34 @@ def build_reference_host():
     return REF_LIB
 
 
+REF_IO_LIB = os.path.join(REF_DIR, "libref_io.so")
+REF_IO_SOURCES = ["gauge_io.c", "spinor_io.c", "cksum.c", "complex.c"]
+
+
+def build_reference_io():
+    """The reference's file code (gauge_io.c, spinor_io.c, cksum.c) with libgfx's
+    LIME implementation standing in for c-lime, plus ref_io_driver.c."""
+    if not all(os.path.exists(os.path.join(REFERENCE, f)) for f in REF_IO_SOURCES):
+        return REF_IO_LIB if os.path.exists(REF_IO_LIB) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    repo = os.path.dirname(HERE)
+    lime = os.path.join(repo, "cudagfx_gb300", "csrc", "gfx_lime.cpp")
+    srcs = [os.path.join(REFERENCE, f) for f in REF_IO_SOURCES]
+    drv = [os.path.join(HERE, "ref_io_driver.c"), os.path.join(HERE, "ref_globals.c")]
+    if _newer(REF_IO_LIB, srcs + drv + [lime, os.path.join(repo, "include", "lime.h"), __file__]):
+        cuda_inc = "/usr/local/cuda/include"
+        inc = ["-I" + REFERENCE, "-I" + os.path.join(repo, "include"), "-I" + cuda_inc]
+        lime_obj = os.path.join(REF_DIR, "gfx_lime.o")
+        _run(["g++", "-O2", "-fPIC", "-std=c++17", "-c", lime, "-o", lime_obj] + inc)
+        _run(["gcc", "-O2", "-shared", "-fPIC", "-w", "-std=gnu99"] + inc + srcs + drv +
+             [lime_obj, "-o", REF_IO_LIB, "-lstdc++", "-lm"])
+    return REF_IO_LIB
+
+
 def build():
     build_oracle()
     build_reference_host()
+    build_reference_io()
 
 
 if __name__ == "__main__":

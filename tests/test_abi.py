@@ -24,7 +24,7 @@ def _declared(header):
     return funcs, globs
 
 
-@pytest.mark.parametrize("header", ["gfx.h", "gfx_legacy.h"])
+@pytest.mark.parametrize("header", ["gfx.h", "gfx_legacy.h", "gfx_io.h", "lime.h"])
 def test_every_declared_symbol_is_exported(gfx, header):
     funcs, globs = _declared(header)
     assert len(funcs) > 10 if header == "gfx.h" else len(funcs) > 8
