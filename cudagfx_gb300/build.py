@@ -110,11 +110,30 @@ def _build_locked(verbose, force, ptxas_info):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
+    _build_program(verbose, force or bool(jobs))
     if ptxas_info:
         for u, e in logs.items():
             if e:
                 print("== %s\n%s" % (u, e))
     return LIB
+
+
+PROGRAM = os.path.join(HERE, "gfx_gaugefix")
+
+
+def _build_program(verbose, force):
+    """host/gfx_gaugefix.c -> gfx_gaugefix, linked against libgfx.so next to it"""
+    src = os.path.join(HERE, "host", "gfx_gaugefix.c")
+    if not force and os.path.exists(PROGRAM) and not _stale(PROGRAM, src, _headers()):
+        return PROGRAM
+    cmd = ["gcc", "-O2", "-std=gnu99", "-Wall", "-I" + INCLUDE, src, "-o", PROGRAM,
+           "-L" + HERE, "-lgfx", "-Wl,-rpath,$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("program link failed: %s\n%s" % (r.stdout, r.stderr))
+    return PROGRAM
 
 
 if __name__ == "__main__":

@@ -280,6 +280,15 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   return GFX_OK;
 }
 
+gfx_status gfx_set_device(int device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(nullptr, GFX_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+  }
+  return GFX_OK;
+}
+
 gfx_status gfx_synchronize(gfx_ctx* ctx) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
   CK(cudaStreamSynchronize(ctx->stream));

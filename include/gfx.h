@@ -122,6 +122,10 @@ const char *gfx_status_string(int status);
 /* last error message of this context (or the global one when ctx is NULL) */
 const char *gfx_last_error(const gfx_ctx *ctx);
 
+/* cudaSetDevice for C callers that do not link the CUDA runtime themselves
+ * (the reference's main selects its card with -d, cudagaugefix.cu:628-661) */
+gfx_status gfx_set_device(int device);
+
 /* Create a context on the current device.  link_reals64 = 12 (two-row storage,
  * the reference layout) or 18 (full matrices) for the FP64 link copy.
  * stream = a cudaStream_t to run on, or NULL for a private stream. */

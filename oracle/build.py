@@ -92,6 +92,29 @@ def build_reference_io():
     return REF_IO_LIB
 
 
+REF_PROGRAM = os.path.join(REF_DIR, "ref_gaugefix")
+REF_LINK_SOURCES = ["read_input.c", "gauge_io.c", "spinor_io.c", "cksum.c", "su3manip.c",
+                    "observables.c", "rngs.c", "complex.c"]
+
+
+def build_reference_link():
+    """The reference's host C files, unchanged, with ref_link_main.c, linked against
+    libgfx.so: the program the reference's main is, with libgfx as its CUDA side."""
+    if not all(os.path.exists(os.path.join(REFERENCE, f)) for f in REF_LINK_SOURCES):
+        return REF_PROGRAM if os.path.exists(REF_PROGRAM) else None
+    os.makedirs(REF_DIR, exist_ok=True)
+    repo = os.path.dirname(HERE)
+    pkg = os.path.join(repo, "cudagfx_gb300")
+    libgfx = os.path.join(pkg, "libgfx.so")
+    srcs = [os.path.join(REFERENCE, f) for f in REF_LINK_SOURCES]
+    main = os.path.join(HERE, "ref_link_main.c")
+    if _newer(REF_PROGRAM, srcs + [main, libgfx, __file__]):
+        inc = ["-I" + REFERENCE, "-I" + os.path.join(repo, "include"), "-I/usr/local/cuda/include"]
+        _run(["gcc", "-O2", "-w", "-std=gnu99"] + inc + srcs + [main, "-o", REF_PROGRAM,
+             "-L" + pkg, "-lgfx", "-Wl,-rpath," + pkg, "-lm"])
+    return REF_PROGRAM
+
+
 def build():
     build_oracle()
     build_reference_host()
