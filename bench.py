@@ -454,7 +454,9 @@ def run_gfx(args, dims):
             "bytes_per_launch": bytes32,
             "time_share_in_solve": t32_share / max(r_last.ms, 1e-9)}
     if ms64:
-        roof["fp64_kernel"] = {"kernel": "or_halfsweep_kernel<double,12,4>", "ms_per_launch": ms64,
+        nr64 = tune64["link_reals64"] if tune64 else 12
+        roof["fp64_kernel"] = {"kernel": "or_halfsweep_kernel<double,%d,4>" % nr64,
+                               "ms_per_launch": ms64,
                                "gflops": FLOP_PER_UPDATE * V / 2 / (ms64 / 1000.0) / 1e9,
                                "time_share_in_solve": t64_share / max(r_last.ms, 1e-9)}
 
