@@ -105,12 +105,13 @@ class ThermParams(_c.Structure):
 
 class Tuning(_c.Structure):
     _fields_ = [("block", _c.c_int * 2), ("staging", _c.c_int * 2), ("link_reals64", _c.c_int),
-                ("checkinterval", _c.c_int), ("sweep_ms", _c.c_double * 2),
-                ("check_ms", _c.c_double * 2)]
+                ("link_reals32", _c.c_int), ("checkinterval", _c.c_int),
+                ("sweep_ms", _c.c_double * 2), ("check_ms", _c.c_double * 2)]
 
     def as_dict(self):
         return {"block": list(self.block), "staging": list(self.staging),
-                "link_reals64": self.link_reals64, "checkinterval": self.checkinterval,
+                "link_reals64": self.link_reals64, "link_reals32": self.link_reals32,
+                "checkinterval": self.checkinterval,
                 "sweep_ms": list(self.sweep_ms), "check_ms": list(self.check_ms)}
 
 
@@ -291,12 +292,14 @@ class Context:
         self._check(lib.gfx_get_tuning(self._h, _c.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0):
+    def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0,
+                   link_reals32=0):
         """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first."""
         t = Tuning()
         t.block[0], t.block[1] = block
         t.staging[0], t.staging[1] = staging
         t.link_reals64 = link_reals64
+        t.link_reals32 = link_reals32
         t.checkinterval = checkinterval
         self._check(lib.gfx_set_tuning(self._h, _c.byref(t)))
 

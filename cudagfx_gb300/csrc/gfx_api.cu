@@ -30,7 +30,9 @@ struct gfx_ctx {
   long long vol;
   Lattice L;
   int precision;
-  int link_nr;  // FP64 link storage: 12 or 18
+  int link_nr;    // FP64 link storage: 12 or 18
+  int link_nr32;  // FP32 link copy: 12 or 8
+  size_t u32_bytes;
   int block;
   int or_block[2];  // OR/SA half-sweep block size, FP32 [0] and FP64 [1]
   int or_pf[2];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
@@ -117,6 +119,13 @@ static size_t link_bytes64(const gfx_ctx* c) {
 static size_t link_bytes32(const gfx_ctx* c) { return (size_t)8 * 3 * 16 * (size_t)c->L.vh; }
 static size_t g_bytes64(const gfx_ctx* c) { return (size_t)2 * 6 * 16 * (size_t)c->L.vh; }
 static size_t g_bytes32(const gfx_ctx* c) { return (size_t)2 * 3 * 16 * (size_t)c->L.vh; }
+// the layout of the link field that precision prec reads
+static int lnr(const gfx_ctx* c, int prec) { return prec == 0 ? c->link_nr32 : c->link_nr; }
+// FP32 links: 12 reals = 3 planes of 16 bytes; 8 reals = 2 planes + the 3 planes of
+// exact rows kept for the links the 8-parameter form declines
+static size_t link_bytes32_for(const gfx_ctx* c, int nr32) {
+  return (size_t)8 * (nr32 == 8 ? 5 : 3) * 16 * (size_t)c->L.vh;
+}
 
 static gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes) {
   if (ctx->scratch_bytes >= bytes) return GFX_OK;
@@ -156,6 +165,15 @@ static void destroy_graphs(gfx_ctx* ctx) {
     cudaGraphDestroy(g.graph);
   }
   ctx->graphs.clear();
+}
+
+// the FP32 link copy from the FP64 links, in the current FP32 layout
+static gfx_status refresh_u32(gfx_ctx* ctx) {
+  if (!ctx->U32) return GFX_OK;
+  launch_convert_links_64_to_32(ctx->link_nr, ctx->link_nr32, ctx->L, ctx->U64, ctx->U32,
+                                ctx->stream);
+  CK(cudaGetLastError());
+  return GFX_OK;
 }
 
 gfx_status gfx_destroy(gfx_ctx* ctx) {
@@ -200,6 +218,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->L = make_lattice(lx, ly, lz, lt);
   ctx->precision = precision;
   ctx->link_nr = link_reals64;
+  ctx->link_nr32 = 12;
   ctx->block = 128;
   ctx->or_block[0] = ctx->or_block[1] = 128;
   ctx->or_pf[0] = ctx->or_pf[1] = 0;
@@ -247,6 +266,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   TRY(dalloc(ctx, &ctx->G64, g_bytes64(ctx)));
   if (precision != GFX_PREC_DOUBLE) {
     TRY(dalloc(ctx, &ctx->U32, link_bytes32(ctx)));
+    ctx->u32_bytes = link_bytes32(ctx);
     TRY(dalloc(ctx, &ctx->G32, g_bytes32(ctx)));
   }
   // measurement partials: 3 doubles per block, blocks of >= 64 threads
@@ -318,7 +338,10 @@ gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
   if (s) return s;
   CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
   launch_pack_links(ctx->link_nr, ctx->L, ctx->scratch_aos, ctx->U64, ctx->stream);
-  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  if (ctx->U32) {
+    gfx_status rs = refresh_u32(ctx);
+    if (rs) return rs;
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return GFX_OK;
@@ -410,7 +433,7 @@ static void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
   const void* U = prec == 0 ? ctx->U32 : ctx->U64;
   void* G = prec == 0 ? ctx->G32 : ctx->G64;
   for (int p = 0; p < 2; p++)
-    launch_or_halfsweep(prec, ctx->link_nr, ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
+    launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
                         ctx->or_pf[prec], ctx->stream);
   ctx->launches += 2;
 }
@@ -430,7 +453,7 @@ static void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
   const int b = meas_block(ctx);
   const void* U = cprec == 0 ? ctx->U32 : ctx->U64;
   const void* G = gprec == 0 ? ctx->G32 : ctx->G64;
-  launch_measure(cprec, ctx->link_nr, gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
+  launch_measure(cprec, lnr(ctx, cprec), gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
   ctx->launches += 1;
 }
 
@@ -450,7 +473,7 @@ gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, i
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
-  launch_or_halfsweep(prec, ctx->link_nr, ndir, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
+  launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
                       prec == 0 ? ctx->G32 : ctx->G64, parity, omega, ctx->or_block[prec],
                       ctx->or_pf[prec], ctx->stream);
   CK(cudaGetLastError());
@@ -521,7 +544,10 @@ gfx_status gfx_apply_trafo(gfx_ctx* ctx) {
   gfx_status s = sync_g64(ctx);
   if (s) return s;
   launch_apply_trafo(ctx->link_nr, ctx->L, ctx->U64, ctx->G64, ctx->stream);
-  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  if (ctx->U32) {
+    gfx_status rs = refresh_u32(ctx);
+    if (rs) return rs;
+  }
   CK(cudaGetLastError());
   return gfx_unit_trafo(ctx);
 }
@@ -961,7 +987,7 @@ gfx_status gfx_sa_halfsweep(gfx_ctx* ctx, int parity, double beta, int precision
   if (s) return s;
   const int prec = precision == 0 ? 0 : 1;
   if ((s = prepare_g(ctx, prec))) return s;
-  launch_sa_heatbath(prec, ctx->link_nr, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
+  launch_sa_heatbath(prec, lnr(ctx, prec), ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
                      prec == 0 ? ctx->G32 : ctx->G64, parity, beta, ctx->gauss, ctx->unif,
                      ctx->block, ctx->stream);
   CK(cudaGetLastError());
@@ -974,7 +1000,7 @@ gfx_status gfx_micro_halfsweep(gfx_ctx* ctx, int parity, int gauge, int precisio
   const int prec = precision == 0 ? 0 : 1;
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
-  launch_micro(prec, ctx->link_nr, gauge == GFX_GAUGE_COULOMB ? 3 : 4, ctx->L,
+  launch_micro(prec, lnr(ctx, prec), gauge == GFX_GAUGE_COULOMB ? 3 : 4, ctx->L,
                prec == 0 ? ctx->U32 : ctx->U64, prec == 0 ? ctx->G32 : ctx->G64, parity,
                ctx->block, ctx->stream);
   CK(cudaGetLastError());
@@ -996,13 +1022,13 @@ gfx_status gfx_simanneal_range(gfx_ctx* ctx, const gfx_sa_params* p, int first, 
     // set_sa_temperature: beta = 1/T (simulated_annealing.cu:292)
     const double beta = 1.0 / gfx_sa_temperature(p, i);
     for (int par = 0; par < 2; par++) {
-      launch_sa_heatbath(prec, ctx->link_nr, ctx->L, U, G, par, beta, ctx->gauss, ctx->unif,
+      launch_sa_heatbath(prec, lnr(ctx, prec), ctx->L, U, G, par, beta, ctx->gauss, ctx->unif,
                          ctx->block, ctx->stream);
       enqueue_mt_update(ctx);
     }
     for (int m = 0; m < p->nmicro; m++)
       for (int par = 0; par < 2; par++)
-        launch_micro(prec, ctx->link_nr, 4, ctx->L, U, G, par, ctx->block, ctx->stream);
+        launch_micro(prec, lnr(ctx, prec), 4, ctx->L, U, G, par, ctx->block, ctx->stream);
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -1028,7 +1054,10 @@ gfx_status gfx_link_heatbath_halfsweep(gfx_ctx* ctx, int parity, int nu, double 
     return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
   launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, parity, nu, beta / 3.0, ctx->gauss,
                        ctx->unif, variant, 128, ctx->stream);
-  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  if (ctx->U32) {
+    gfx_status rs = refresh_u32(ctx);
+    if (rs) return rs;
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return GFX_OK;
@@ -1058,7 +1087,10 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
       np++;
     }
   }
-  if (ctx->U32) launch_convert_links_64_to_32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, ctx->stream);
+  if (ctx->U32) {
+    gfx_status rs = refresh_u32(ctx);
+    if (rs) return rs;
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return GFX_OK;
@@ -1334,6 +1366,7 @@ gfx_status gfx_get_tuning(const gfx_ctx* ctx, gfx_tuning* t) {
     t->check_ms[p] = ctx->tune_measure_ms[p];
   }
   t->link_reals64 = ctx->link_nr;
+  t->link_reals32 = ctx->link_nr32;
   t->checkinterval = ctx->tune_ck;
   return GFX_OK;
 }
@@ -1363,6 +1396,28 @@ static gfx_status relayout_links(gfx_ctx* ctx, int nr) {
 
 static bool valid_block(int b) { return b >= 32 && b <= 256 && b % 32 == 0; }
 
+// FP32 link layout 12 or 8; the 8-real copy needs a larger buffer (allocated first)
+static gfx_status set_link_layout32(gfx_ctx* ctx, int nr32) {
+  if (!ctx->U32 || nr32 == ctx->link_nr32) return GFX_OK;
+  const size_t need = link_bytes32_for(ctx, nr32);
+  if (need > ctx->u32_bytes) {
+    void* nu = nullptr;
+    gfx_status s = dalloc(ctx, &nu, need);
+    if (s) return s;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->U32);
+    ctx->dev_bytes -= ctx->u32_bytes;
+    ctx->U32 = nu;
+    ctx->u32_bytes = need;
+  }
+  ctx->link_nr32 = nr32;
+  destroy_graphs(ctx);
+  gfx_status s = refresh_u32(ctx);
+  if (s) return s;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
 gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
   if (!ctx || !t) return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: NULL argument");
   for (int p = 0; p < 2; p++) {
@@ -1374,8 +1429,14 @@ gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
   if (t->link_reals64 != 0 && t->link_reals64 != 12 && t->link_reals64 != 18)
     return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals64 must be 0, 12 or 18");
   if (t->checkinterval < 0) return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: checkinterval < 0");
+  if (t->link_reals32 != 0 && t->link_reals32 != 12 && t->link_reals32 != 8)
+    return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals32 must be 0, 12 or 8");
   if (t->link_reals64) {
     gfx_status s = relayout_links(ctx, t->link_reals64);
+    if (s) return s;
+  }
+  if (t->link_reals32 && t->link_reals32 != ctx->link_nr32 && ctx->U32) {
+    gfx_status s = set_link_layout32(ctx, t->link_reals32);
     if (s) return s;
   }
   for (int p = 0; p < 2; p++) {
@@ -1424,7 +1485,8 @@ static std::string tune_key(const gfx_ctx* ctx, int ndir) {
   return key;
 }
 
-// cache line: key TAB block0 staging0 block1 staging1 link_reals64 sweep_ms0 sweep_ms1 check_ms0 check_ms1
+// cache line: key TAB block0 staging0 block1 staging1 link_reals64 link_reals32 sweep_ms0
+// sweep_ms1 check_ms0 check_ms1
 static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t) {
   FILE* f = std::fopen(path, "r");
   if (!f) return false;
@@ -1435,9 +1497,10 @@ static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t
     if (!tab || std::string(line, tab - line) != key) continue;
     gfx_tuning c;
     std::memset(&c, 0, sizeof(c));
-    if (std::sscanf(tab + 1, "%d %d %d %d %d %lf %lf %lf %lf", &c.block[0], &c.staging[0],
-                    &c.block[1], &c.staging[1], &c.link_reals64, &c.sweep_ms[0], &c.sweep_ms[1],
-                    &c.check_ms[0], &c.check_ms[1]) == 9 &&
+    if (std::sscanf(tab + 1, "%d %d %d %d %d %d %lf %lf %lf %lf", &c.block[0], &c.staging[0],
+                    &c.block[1], &c.staging[1], &c.link_reals64, &c.link_reals32, &c.sweep_ms[0],
+                    &c.sweep_ms[1], &c.check_ms[0], &c.check_ms[1]) == 10 &&
+        (c.link_reals32 == 12 || c.link_reals32 == 8) &&
         valid_block(c.block[0]) && valid_block(c.block[1]) &&
         (c.link_reals64 == 12 || c.link_reals64 == 18)) {
       *t = c;  // the last valid line for a key wins
@@ -1451,9 +1514,9 @@ static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t
 static void cache_append(const char* path, const std::string& key, const gfx_tuning& t) {
   FILE* f = std::fopen(path, "a");
   if (!f) return;  // the cache is an optimisation; an unwritable path only costs a re-tune
-  std::fprintf(f, "%s\t%d %d %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), t.block[0],
-               t.staging[0], t.block[1], t.staging[1], t.link_reals64, t.sweep_ms[0],
-               t.sweep_ms[1], t.check_ms[0], t.check_ms[1]);
+  std::fprintf(f, "%s\t%d %d %d %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), t.block[0],
+               t.staging[0], t.block[1], t.staging[1], t.link_reals64, t.link_reals32,
+               t.sweep_ms[0], t.sweep_ms[1], t.check_ms[0], t.check_ms[1]);
   std::fclose(f);
 }
 
@@ -1502,13 +1565,19 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
   for (int prec = 0; prec < 2 && s == GFX_OK; prec++) {
     if (prec == 0 && !ctx->G32) continue;
     if (prec == 1 && ctx->precision == GFX_PREC_SINGLE) continue;  // FP64 sweeps never run
-    const int layouts[2] = {ctx->link_nr, ctx->link_nr == 12 ? 18 : 12};
-    const int nlayouts = prec == 1 ? 2 : 1;
+    // link layouts: FP64 12/18 reals, FP32 12/8 reals
+    int layouts[2] = {ctx->link_nr, ctx->link_nr == 12 ? 18 : 12};
+    const int nlayouts = 2;
+    if (prec == 0) {
+      layouts[0] = 12;
+      layouts[1] = 8;
+    }
     double best = 1e30;
-    int bb = ctx->or_block[prec], bp = ctx->or_pf[prec], bnr = ctx->link_nr;
+    int bb = ctx->or_block[prec], bp = ctx->or_pf[prec], bnr = layouts[0];
     int n = 0;
     for (int li = 0; li < nlayouts && s == GFX_OK; li++) {
       if (prec == 1 && (s = relayout_links(ctx, layouts[li]))) break;
+      if (prec == 0 && (s = set_link_layout32(ctx, layouts[li]))) break;
       if ((s = prepare_g(ctx, prec))) break;
       if (n == 0) {
         double t1 = 0.0;
@@ -1529,7 +1598,7 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
               best = ms;
               bb = blocks[bi];
               bp = pf;
-              bnr = ctx->link_nr;
+              bnr = layouts[li];
             }
           }
     }
@@ -1537,6 +1606,7 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
     ctx->or_block[prec] = bb;
     ctx->or_pf[prec] = bp;
     if (prec == 1 && (s = relayout_links(ctx, bnr))) break;
+    if (prec == 0 && (s = set_link_layout32(ctx, bnr))) break;
     ctx->tune_sweep_ms[prec] = best;
     if ((s = prepare_g(ctx, prec))) break;
     auto check = [&]() {

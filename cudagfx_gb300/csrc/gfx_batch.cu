@@ -507,7 +507,7 @@ gfx_status gfx_batch_set_links(gfx_batch* b, int conf, const double* su3) {
   BCK(cudaMallocAsync((void**)&scratch, bytes, b->stream));
   BCK(cudaMemcpyAsync(scratch, su3, bytes, cudaMemcpyHostToDevice, b->stream));
   launch_pack_links(12, C.L, scratch, (void*)C.U64, b->stream);
-  if (C.U32) launch_convert_links_64_to_32(12, C.L, C.U64, (void*)C.U32, b->stream);
+  if (C.U32) launch_convert_links_64_to_32(12, 12, C.L, C.U64, (void*)C.U32, b->stream);
   BCK(cudaFreeAsync(scratch, b->stream));
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(b->stream));

@@ -351,7 +351,9 @@ struct VecOf<double> {
 template <typename T, int NR>
 struct Field {
   typedef typename VecOf<T>::type V;
-  static constexpr int NCHUNK = NR * (int)sizeof(T) / 16;
+  // FP32 8-real links keep their exact 12-real rows in three more planes for the
+  // links the 8-parameter form cannot hold accurately (see reconstruct8): 5 planes
+  static constexpr int NCHUNK = NR == 8 ? 5 : NR * (int)sizeof(T) / 16;
 
   // load matrix i of the block starting at base (planes spaced by stride vectors)
   __device__ static __forceinline__ void load(const V* __restrict__ base, size_t stride, int i,
@@ -384,6 +386,67 @@ template <>
 __device__ __forceinline__ void Field<float, 12>::load(const float4* __restrict__ base,
                                                        size_t stride, int i, Mat3<float>& m) {
   unpack12(__ldg(base + i), __ldg(base + stride + i), __ldg(base + 2 * stride + i), m);
+}
+
+// 8-real links (the reference's GF_8 parameters, su3manip.c:234-276):
+//   p = (a2, a3), q = (arg a1, arg c1, b1) for rows a, b, c.
+// |a1| = sqrt(1 - |a2|^2 - |a3|^2) and |c1| = sqrt(1 - |a1|^2 - |b1|^2) from the unit
+// first row and column.  b2, b3 follow from b orthogonal to a and conj(c1) = a2 b3 - a3 b2
+// (c = conj(a x b)); c2, c3 from c orthogonal to a and conj(b1) = c2 a3 - c3 a2; each a 2x2
+// system with determinant |a2|^2 + |a3|^2.  The layout cannot hold links with
+// |a2|^2 + |a3|^2 near 0 (e.g. unit links; the FP32 error grows like 6e-8 over it):
+// returns false below kMinN2For8, and the caller reads the exact 12-real rows.
+constexpr float kMinN2For8 = 1e-2f;
+__device__ __forceinline__ bool reconstruct8(float4 p, float4 q, Mat3<float>& m) {
+  const cplx<float> a2 = cmk(p.x, p.y), a3 = cmk(p.z, p.w), b1 = cmk(q.z, q.w);
+  const float n2 = fm(p.w, p.w, fm(p.z, p.z, fm(p.y, p.y, p.x * p.x)));
+  if (n2 < kMinN2For8) return false;
+  // hardware approximations (a few FP32 ulp): this copy only feeds the FP32 sweeps
+  const float x1 = fmaxf(1.0f - n2, 0.0f);
+  const float xc = fmaxf(n2 - fm(b1.im, b1.im, b1.re * b1.re), 0.0f);
+  const float r1 = x1 > 0.0f ? x1 * rsqrtf(x1) : 0.0f;
+  const float rc = xc > 0.0f ? xc * rsqrtf(xc) : 0.0f;
+  float s1, c1s, s3, c3s;
+  __sincosf(q.x, &s1, &c1s);
+  __sincosf(q.y, &s3, &c3s);
+  const cplx<float> a1 = cmk(r1 * c1s, r1 * s1), c1 = cmk(rc * c3s, rc * s3);
+  const float inv = __fdividef(1.0f, n2);
+  const cplx<float> ca1b1 = cmulc(b1, a1);  // conj(a1) b1
+  const cplx<float> ca1c1 = cmulc(c1, a1);  // conj(a1) c1
+  const cplx<float> cc1 = cconj(c1), cb1 = cconj(b1), ca2 = cconj(a2), ca3 = cconj(a3);
+  cplx<float> t;
+  t = cmul(a2, ca1b1);
+  cmac(t, ca3, cc1);
+  const cplx<float> b2 = cmk(-t.re * inv, -t.im * inv);
+  t = cmul(ca2, cc1);
+  t = csub(t, cmul(a3, ca1b1));
+  const cplx<float> b3 = cmk(t.re * inv, t.im * inv);
+  t = cmul(ca3, cb1);
+  t = csub(t, cmul(a2, ca1c1));
+  const cplx<float> c2 = cmk(t.re * inv, t.im * inv);
+  t = cmul(ca2, cb1);
+  cmac(t, a3, ca1c1);
+  const cplx<float> c3 = cmk(-t.re * inv, -t.im * inv);
+  m.e[0][0] = a1;
+  m.e[0][1] = a2;
+  m.e[0][2] = a3;
+  m.e[1][0] = b1;
+  m.e[1][1] = b2;
+  m.e[1][2] = b3;
+  m.e[2][0] = c1;
+  m.e[2][1] = c2;
+  m.e[2][2] = c3;
+  return true;
+}
+
+// planes 0, 1: the 8 parameters; planes 2-4: rows 0, 1 as in the 12-real layout,
+// read only for the rare links reconstruct8 declines
+template <>
+__device__ __forceinline__ void Field<float, 8>::load(const float4* __restrict__ base,
+                                                      size_t stride, int i, Mat3<float>& m) {
+  if (!reconstruct8(__ldg(base + i), __ldg(base + stride + i), m))
+    unpack12(__ldg(base + 2 * stride + i), __ldg(base + 3 * stride + i),
+             __ldg(base + 4 * stride + i), m);
 }
 
 

@@ -178,7 +178,10 @@ void launch_sa_heatbath(int prec, int link_nr, const Lattice& L, const void* U, 
                         cudaStream_t s) {
   dim3 grid((L.vh + block - 1) / block);
   const float4* u4 = (const float4*)unif;
-  if (prec == 0)
+  if (prec == 0 && link_nr == 8)
+    sa_heatbath_kernel<float, 8><<<grid, block, 0, s>>>(L, (const float4*)U, (float4*)G, parity,
+                                                         beta, gauss, u4);
+  else if (prec == 0)
     sa_heatbath_kernel<float, 12><<<grid, block, 0, s>>>(L, (const float4*)U, (float4*)G, parity,
                                                           beta, gauss, u4);
   else if (link_nr == 18)
@@ -195,7 +198,10 @@ void launch_micro(int prec, int link_nr, int ndir, const Lattice& L, const void*
 #define MICRO(T, NR, ND)                                                        \
   micro_kernel<T, NR, ND><<<grid, block, 0, s>>>(L, (const typename VecOf<T>::type*)U, \
                                                    (typename VecOf<T>::type*)G, parity)
-  if (prec == 0) {
+  if (prec == 0 && link_nr == 8) {
+    if (ndir == 4) MICRO(float, 8, 4);
+    else MICRO(float, 8, 3);
+  } else if (prec == 0) {
     if (ndir == 4) MICRO(float, 12, 4);
     else MICRO(float, 12, 3);
   } else if (link_nr == 18) {

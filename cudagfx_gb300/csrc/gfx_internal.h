@@ -44,7 +44,8 @@ struct Reduced {
 };
 
 // ----- kernel launchers (gfx_kernels.cu) -----
-// precision tags: 0 = FP32 12-real, 1 = FP64 12-real, 2 = FP64 18-real (links only)
+// link_nr arguments give the layout of the link field read: FP32 12 or 8 reals when
+// prec == 0, FP64 12 or 18 reals otherwise
 // mode: 0 plain loads, 1 L2 bulk prefetch per block
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
                          int parity, double omega, int block, int mode, cudaStream_t s);
@@ -65,8 +66,9 @@ void launch_unpack_links(int link_nr_prec, const Lattice& L, const void* U, doub
                          cudaStream_t s);
 void launch_pack_g(int gprec, const Lattice& L, const double* aos, void* G, cudaStream_t s);
 void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cudaStream_t s);
-void launch_convert_links_64_to_32(int link_nr, const Lattice& L, const void* U64, void* U32,
-                                   cudaStream_t s);
+// link_nr32: FP32 layout of the copy, 12 or 8 reals
+void launch_convert_links_64_to_32(int link_nr, int link_nr32, const Lattice& L, const void* U64,
+                                   void* U32, cudaStream_t s);
 void launch_convert_g(int from_prec, int to_prec, const Lattice& L, const void* Gin, void* Gout,
                       cudaStream_t s);
 void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s);

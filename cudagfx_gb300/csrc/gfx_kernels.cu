@@ -80,7 +80,10 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
     else                                                                                         \
       or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
   } while (0)
-  if (prec == 0) {
+  if (prec == 0 && link_nr == 8) {
+    if (ndir == 4) OR_LAUNCH(float, 8, 4);
+    else OR_LAUNCH(float, 8, 3);
+  } else if (prec == 0) {
     if (ndir == 4) OR_LAUNCH(float, 12, 4);
     else OR_LAUNCH(float, 12, 3);
   } else if (link_nr == 18) {
@@ -132,7 +135,10 @@ void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& 
   measure_kernel<TC, TSU, NR, TSG, ND><<<grid, block, 0, s>>>(                      \
       L, (const typename VecOf<TSU>::type*)U, (const typename VecOf<TSG>::type*)G, \
       partials)
-  if (cprec == 0) {
+  if (cprec == 0 && link_nr == 8) {
+    if (ndir == 4) MEAS(float, float, 8, float, 4);
+    else MEAS(float, float, 8, float, 3);
+  } else if (cprec == 0) {
     if (ndir == 4) MEAS(float, float, 12, float, 4);
     else MEAS(float, float, 12, float, 3);
   } else if (gprec == 0) {
@@ -454,7 +460,9 @@ void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cu
   else unpack_g_kernel<double><<<grid, 128, 0, s>>>(L, (const double2*)G, aos);
 }
 
-template <int NR>
+// FP32 copy of the links: 12 reals (rows 0, 1) or 8 (a2, a3, arg a1, arg c1, b1; the
+// angles by atan2 in FP64 as su3to8 does, su3manip.c:234-253)
+template <int NR, int NR32>
 __global__ void links_64_to_32_kernel(Lattice L, const double2* U64, float4* U32) {
   const int blk = blockIdx.y;  // parity*4 + mu
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -466,16 +474,31 @@ __global__ void links_64_to_32_kernel(Lattice L, const double2* U64, float4* U32
   for (int r = 0; r < 3; r++)
 #pragma unroll
     for (int c = 0; c < 3; c++) f.e[r][c] = cmk<float>((float)m.e[r][c].re, (float)m.e[r][c].im);
+  if (NR32 == 8) {
+    float4* o = U32 + (size_t)blk * 5 * L.vh;
+    o[i] = make_float4((float)m.e[0][1].re, (float)m.e[0][1].im, (float)m.e[0][2].re,
+                       (float)m.e[0][2].im);
+    o[(size_t)L.vh + i] =
+        make_float4((float)atan2(m.e[0][0].im, m.e[0][0].re), (float)atan2(m.e[2][0].im, m.e[2][0].re),
+                    (float)m.e[1][0].re, (float)m.e[1][0].im);
+    Field<float, 12>::store(o + 2 * (size_t)L.vh, (size_t)L.vh, i, f);  // the exact rows
+    return;
+  }
   Field<float, 12>::store(U32 + (size_t)blk * 3 * L.vh, (size_t)L.vh, i, f);
 }
 
-void launch_convert_links_64_to_32(int link_nr, const Lattice& L, const void* U64, void* U32,
-                                   cudaStream_t s) {
+void launch_convert_links_64_to_32(int link_nr, int link_nr32, const Lattice& L, const void* U64,
+                                   void* U32, cudaStream_t s) {
   dim3 grid((L.vh + 127) / 128, 8);
-  if (link_nr == 18)
-    links_64_to_32_kernel<18><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)U32);
-  else
-    links_64_to_32_kernel<12><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)U32);
+  const double2* u = (const double2*)U64;
+  float4* o = (float4*)U32;
+  if (link_nr == 18) {
+    if (link_nr32 == 8) links_64_to_32_kernel<18, 8><<<grid, 128, 0, s>>>(L, u, o);
+    else links_64_to_32_kernel<18, 12><<<grid, 128, 0, s>>>(L, u, o);
+  } else {
+    if (link_nr32 == 8) links_64_to_32_kernel<12, 8><<<grid, 128, 0, s>>>(L, u, o);
+    else links_64_to_32_kernel<12, 12><<<grid, 128, 0, s>>>(L, u, o);
+  }
 }
 
 // g precision change; widening reunitarizes in FP64

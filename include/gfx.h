@@ -145,7 +145,12 @@ gfx_status gfx_set_block(gfx_ctx *ctx, int block);
  * staging: 0 = plain 128-bit loads; 1 = each block first issues one L2 bulk
  * prefetch (cp.async.bulk.prefetch.L2) per contiguous range it reads.  All
  * settings give bit-identical results.
- * link_reals64: FP64 link storage, 12 (two rows) or 18 (full).
+ * link_reals64: FP64 link storage, 12 (two rows) or 18 (full).  link_reals32: the
+ * FP32 copy the FP32 sweeps read, 12 or 8.  The 8-real form rebuilds rows 1, 2
+ * dividing by |U_01|^2 + |U_02|^2; the few links where that is below 1e-2 are read
+ * from exact rows kept beside it, so every link is accurate to FP32 rounding and
+ * 32 bytes per link are read.  The FP64 links stay exact: the 8-real copy changes
+ * FP32 sweeps at rounding level only; all other settings give bit-identical results.
  * checkinterval: sweeps per convergence check the tuner suggests for the FP32
  * phase (0 = no suggestion).  sweep_ms / check_ms: the tuner's timings of one full
  * sweep and of one check at the chosen settings (0 when set by hand). */
@@ -153,6 +158,8 @@ typedef struct {
   int block[2];
   int staging[2];
   int link_reals64;
+  int link_reals32; /* FP32 link copy: 12, or 8 (the GF_8 parameters a2, a3, arg a1,
+                       arg c1, b1, dev_su3.cu:428-728); 0 = keep */
   int checkinterval;
   double sweep_ms[2];
   double check_ms[2];
@@ -164,7 +171,7 @@ gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
 gfx_status gfx_set_tuning(gfx_ctx *ctx, const gfx_tuning *t);
 /* Time every candidate setting on this context's lattice and apply the fastest.
  * Candidates: block 64/128/192/256 x staging 0/1 for each precision the
- * context holds, and for FP64 both link layouts.  The fields are left as they
+ * context holds, and both link layouts of each precision.  The fields are left as they
  * were: the candidate sweeps run on g and it is restored afterwards.
  * expected_sweeps > 0 also sets checkinterval to the interval that minimises
  * check time plus the sweeps run past convergence, sqrt(2 n check_ms / sweep_ms),

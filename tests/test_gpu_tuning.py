@@ -47,9 +47,13 @@ def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
     t = b.autotune(expected_sweeps=1000, cache_path=str(tmp_path / "tune.txt"))
     assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1)
     assert t["link_reals64"] in (12, 18) and 5 <= t["checkinterval"] <= 100
+    assert t["link_reals32"] in (12, 8)
     assert t["sweep_ms"][0] > 0 and t["check_ms"][1] > 0
     assert np.array_equal(b.get_trafo(), g0)
     assert np.max(np.abs(b.get_links() - u0)) < 1e-15
+    # every choice but the 8-real FP32 links is bit-identical (those are checked apart)
+    b.set_tuning(block=t["block"], staging=t["staging"], link_reals64=t["link_reals64"],
+                 link_reals32=12)
     rb = b.overrelax(**kw)
     assert (rb.iterations, rb.sweeps_single, rb.sweeps_double) == \
         (ra.iterations, ra.sweeps_single, ra.sweeps_double)
@@ -68,8 +72,8 @@ def test_autotune_cache_hit_applies_stored_settings(tmp_path):
     assert len(lines) == 1 and "8x8x8x12" in lines[0]
     b = _ctx()
     t2 = b.autotune(cache_path=path)
-    assert (t2["block"], t2["staging"], t2["link_reals64"]) == \
-        (t1["block"], t1["staging"], t1["link_reals64"])
+    assert (t2["block"], t2["staging"], t2["link_reals64"], t2["link_reals32"]) == \
+        (t1["block"], t1["staging"], t1["link_reals64"], t1["link_reals32"])
     assert b.tuning()["block"] == t1["block"]
     assert len(open(path).read().splitlines()) == 1  # a hit appends nothing
     b.close()
@@ -78,7 +82,7 @@ def test_autotune_cache_hit_applies_stored_settings(tmp_path):
 def test_set_tuning_rejects_bad_settings():
     c = _ctx()
     for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(2, 0)), dict(staging=(0, -1)),
-                dict(link_reals64=8)):
+                dict(link_reals64=8), dict(link_reals32=18)):
         with pytest.raises(gfx.GfxError):
             c.set_tuning(**bad)
     c.close()
@@ -108,3 +112,35 @@ def test_checkinterval_near_shortens_the_end(prec):
     assert rb.sweeps <= ra.sweeps
     a.close()
     b.close()
+
+
+def test_fp32_link8_matches_link12():
+    """The 8-real FP32 links (GF_8 parameters, exact rows kept for the links the form
+    cannot hold) give the 12-real FP32 sweep to FP32 rounding; links that all take
+    the exact rows (unit links) give it bit for bit."""
+    for links, tol in ((gfx.random_init_haar(8, 4 * V), 3e-5), (gfx.unit_init(4 * V), 0.0)):
+        out = []
+        for nr32 in (12, 8):
+            c = _ctx()
+            c.set_links(links)
+            c.set_tuning(link_reals32=nr32)
+            assert c.tuning()["link_reals32"] == nr32
+            c.or_sweeps(3, omega=1.7, precision=0)
+            out.append(c.get_trafo())
+            c.close()
+        assert np.max(np.abs(out[0] - out[1])) <= tol
+
+
+def test_fp32_link8_solve_reaches_the_same_copy():
+    links = smooth_links(DIMS, 0.9, 21)  # far from the identity: the 8-real form is used
+    kw = dict(maxit=6000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA)
+    res = []
+    for nr32 in (12, 8):
+        c = _ctx()
+        c.set_links(links)
+        c.set_tuning(link_reals32=nr32)
+        r = c.overrelax(**kw)
+        assert r.converged and r.final_values.theta < 1e-12
+        res.append(r.final_values.F)
+        c.close()
+    assert abs(res[0] - res[1]) < 1e-11
