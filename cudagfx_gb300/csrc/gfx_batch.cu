@@ -77,21 +77,11 @@ __global__ void __launch_bounds__(kBatchBlock) or_batch_kernel(BDesc d, int pari
   if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
   const int i = blk * kBatchBlock + threadIdx.x;
   if (i >= C.L.vh) return;
-  const size_t vh = (size_t)C.L.vh;
   const Site s = site_of(C.L, i, parity);
   const V* U = (const V*)(sizeof(T) == 4 ? C.U32 : C.U64);
   V* G = (V*)(sizeof(T) == 4 ? C.G32 : C.G64) +
          (size_t)copy * (sizeof(T) == 4 ? C.gstride32 : C.gstride64);
-  Mat3<T> star;
-  compute_star<T, T, 12, T, 12, NDIR>(C.L, s, parity, U, G, star);
-  V* Gp = G + (size_t)parity * NC * vh;
-  Mat3<T> gold, g, gn;
-  Field<T, 12>::load(Gp, vh, i, gold);
-  g = gold;
-  cm_relax(g, star);
-  normalize<T, true>(g);
-  overrelax_rows01(gn, gold, g, omega);
-  Field<T, 12>::store(Gp, vh, i, gn);
+  or_site_update<T, 12, NDIR>(C.L, s, parity, U, G, i, omega);
 }
 
 // Per-copy functional partials (measure_kernel per copy, same block grouping)

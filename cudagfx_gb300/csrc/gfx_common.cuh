@@ -129,6 +129,113 @@ __device__ __forceinline__ void compute_star(const Lattice& L, const Site& c, in
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 star with fewer operations.  Each term is an SU(3) product P; its rows 0, 1
+// need only rows 0, 1 of one factor, and its row 2 is conj(P_0 x P_1):
+//   forward  P = U_mu(x) g^+(x+mu):  rows 0,1 of U, all of g
+//   backward Q = g(x-mu) U_mu(x-mu): rows 0,1 of g, all of U;  w += Q^+
+// so one factor per term is never reconstructed and a third of its products is
+// replaced by a cross product.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load12_rows01(const float4* __restrict__ base, size_t stride,
+                                              int i, Mat3<float>& m) {
+  const float4 a = __ldg(base + i), b = __ldg(base + stride + i), c = __ldg(base + 2 * stride + i);
+  m.e[0][0] = cmk(a.x, a.y);
+  m.e[0][1] = cmk(a.z, a.w);
+  m.e[0][2] = cmk(b.x, b.y);
+  m.e[1][0] = cmk(b.z, b.w);
+  m.e[1][1] = cmk(c.x, c.y);
+  m.e[1][2] = cmk(c.z, c.w);
+}
+// acc += conj(p q - r s)  and  acc += p q - r s
+__device__ __forceinline__ void acc_cross_conj(cplx<float>& acc, cplx<float> p, cplx<float> q,
+                                               cplx<float> r, cplx<float> s) {
+  acc.re = fm(p.re, q.re, fm(-p.im, q.im, fm(-r.re, s.re, fm(r.im, s.im, acc.re))));
+  acc.im = fm(-p.re, q.im, fm(-p.im, q.re, fm(r.re, s.im, fm(r.im, s.re, acc.im))));
+}
+__device__ __forceinline__ void acc_cross(cplx<float>& acc, cplx<float> p, cplx<float> q,
+                                          cplx<float> r, cplx<float> s) {
+  acc.re = fm(p.re, q.re, fm(-p.im, q.im, fm(-r.re, s.re, fm(r.im, s.im, acc.re))));
+  acc.im = fm(p.re, q.im, fm(p.im, q.re, fm(-r.re, s.im, fm(-r.im, s.re, acc.im))));
+}
+
+template <int NDIR>
+__device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c, int parity,
+                                                 const float4* __restrict__ U,
+                                                 const float4* __restrict__ G,
+                                                 Mat3<float>& star) {
+  const size_t vh = (size_t)L.vh;
+  const int q = 1 - parity;
+  const float4* Gq = G + (size_t)q * 3 * vh;
+  mzero(star);
+#pragma unroll
+  for (int mu = 0; mu < NDIR; mu++) {
+    Mat3<float> a, b;
+    cplx<float> P[2][3];
+    // forward: P = U g^+
+    load12_rows01(U + (size_t)(parity * 4 + mu) * 3 * vh, vh, c.i, a);
+    Field<float, 12>::load(Gq, vh, nb_fwd(L, c, mu), b);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        cplx<float> x = cmulc(a.e[r][0], b.e[j][0]);
+        cmacc(x, a.e[r][1], b.e[j][1]);
+        cmacc(x, a.e[r][2], b.e[j][2]);
+        P[r][j] = x;
+        star.e[r][j] = cadd(star.e[r][j], x);
+      }
+    acc_cross_conj(star.e[2][0], P[0][1], P[1][2], P[0][2], P[1][1]);
+    acc_cross_conj(star.e[2][1], P[0][2], P[1][0], P[0][0], P[1][2]);
+    acc_cross_conj(star.e[2][2], P[0][0], P[1][1], P[0][1], P[1][0]);
+    // backward: Q = g(x-mu) U_mu(x-mu), w += Q^+
+    const int jb = nb_bwd(L, c, mu);
+    load12_rows01(Gq, vh, jb, b);
+    Field<float, 12>::load(U + (size_t)(q * 4 + mu) * 3 * vh, vh, jb, a);
+#pragma unroll
+    for (int r = 0; r < 2; r++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        cplx<float> x = cmul(b.e[r][0], a.e[0][j]);
+        cmac(x, b.e[r][1], a.e[1][j]);
+        cmac(x, b.e[r][2], a.e[2][j]);
+        P[r][j] = x;
+        star.e[j][r] = cadd(star.e[j][r], cconj(x));
+      }
+    // (Q^+)_{j2} = conj(Q_{2j}) = (Q_0 x Q_1)_j
+    acc_cross(star.e[0][2], P[0][1], P[1][2], P[0][2], P[1][1]);
+    acc_cross(star.e[1][2], P[0][2], P[1][0], P[0][0], P[1][2]);
+    acc_cross(star.e[2][2], P[0][0], P[1][1], P[0][1], P[1][0]);
+  }
+}
+
+// One overrelaxation site update (overrelax.cu:335-446) of site i of parity `parity`
+// in place: FP64 in the reference's operation order, FP32 with the reduced forms.
+template <typename T, int NRU, int NDIR>
+__device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, int parity,
+                                               const typename VecOf<T>::type* __restrict__ U,
+                                               typename VecOf<T>::type* __restrict__ G, int i,
+                                               T omega) {
+  constexpr int NCG = Field<T, 12>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  typename VecOf<T>::type* Gp = G + (size_t)parity * NCG * vh;
+  Mat3<T> star, gold, gn;
+  if constexpr (sizeof(T) == 4 && NRU == 12)
+    compute_star_f32<NDIR>(L, c, parity, U, G, star);
+  else
+    compute_star<T, T, NRU, T, 12, NDIR>(L, c, parity, U, G, star);
+  Field<T, 12>::load(Gp, vh, i, gold);
+  if constexpr (sizeof(T) == 4) {
+    or_update_composed(gold, star, omega, gn);
+  } else {
+    Mat3<T> g = gold;
+    cm_relax(g, star);
+    normalize<T, true>(g);
+    overrelax_rows01(gn, gold, g, omega);
+  }
+  Field<T, 12>::store(Gp, vh, i, gn);
+}
+
 // Per-site functional from X = g w (overrelax.cu:451-605, see measure_kernel):
 // f = Re tr X, d = tr[Delta Delta^+] = sum_ij |AH(X)_ij|^2.
 template <typename TC>

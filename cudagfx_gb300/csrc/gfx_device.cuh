@@ -328,6 +328,93 @@ __device__ __forceinline__ void overrelax_rows01(Mat3<T>& gout, const Mat3<T>& g
 }
 
 // ---------------------------------------------------------------------------
+// The same overrelaxation update with fewer operations (used for FP32 sweeps; the
+// FP64 sweeps keep the reference's operation order above).
+// The three subgroup steps act from the left, g_relax = S g_old with
+// S = S3 S2 S1, so R = g_relax g_old^+ - 1 = S - 1, and
+//   Rw g_old = g_old + (w R + w(w-1)/2 R^2) g_old        (rows 0, 1 only).
+// Each subgroup needs four entries of X = S_k..S_1 g_old w; they are carried
+// along by rotating only the entries later subgroups read.
+// ---------------------------------------------------------------------------
+// the unit SU(2) element of subgroup (a,b) from Xaa, Xbb, Xab, Xba as (p, q):
+// rows a,b <- (p row_a + q row_b, -conj(q) row_a + conj(p) row_b)   (overrelax.cu:184-198)
+template <typename T>
+__device__ __forceinline__ void su2_pq(cplx<T> xaa, cplx<T> xbb, cplx<T> xab, cplx<T> xba,
+                                       cplx<T>& p, cplx<T>& q) {
+  const T w0 = xaa.re + xbb.re, w3 = xbb.im - xaa.im, w1 = -xab.im - xba.im,
+          w2 = xba.re - xab.re;
+  const T r = rsqrt_t<T>(fm(w3, w3, fm(w2, w2, fm(w1, w1, w0 * w0))));
+  p = cmk<T>(w0 * r, w3 * r);
+  q = cmk<T>(w2 * r, w1 * r);
+}
+// -conj(q) x + conj(p) y
+template <typename T>
+__device__ __forceinline__ cplx<T> su2_low(cplx<T> p, cplx<T> q, cplx<T> x, cplx<T> y) {
+  cplx<T> r = cmk<T>(-q.re, q.im);  // -conj(q)
+  cplx<T> o = cmul(r, x);
+  cmac(o, cconj(p), y);
+  return o;
+}
+// p x + q y
+template <typename T>
+__device__ __forceinline__ cplx<T> su2_high(cplx<T> p, cplx<T> q, cplx<T> x, cplx<T> y) {
+  cplx<T> o = cmul(p, x);
+  cmac(o, q, y);
+  return o;
+}
+
+template <typename T>
+__device__ __forceinline__ void or_update_composed(const Mat3<T>& gold, const Mat3<T>& star,
+                                                   T omega, Mat3<T>& gn) {
+  Mat3<T> X;
+  mul(X, gold, star);
+  cplx<T> p1, q1, p2, q2, p3, q3;
+  su2_pq(X.e[0][0], X.e[1][1], X.e[0][1], X.e[1][0], p1, q1);  // subgroup (0,1)
+  const cplx<T> x00 = su2_high(p1, q1, X.e[0][0], X.e[1][0]);
+  const cplx<T> x01 = su2_high(p1, q1, X.e[0][1], X.e[1][1]);
+  const cplx<T> x02 = su2_high(p1, q1, X.e[0][2], X.e[1][2]);
+  const cplx<T> x11 = su2_low(p1, q1, X.e[0][1], X.e[1][1]);
+  const cplx<T> x12 = su2_low(p1, q1, X.e[0][2], X.e[1][2]);
+  su2_pq(x00, X.e[2][2], x02, X.e[2][0], p2, q2);  // subgroup (0,2)
+  const cplx<T> y21 = su2_low(p2, q2, x01, X.e[2][1]);
+  const cplx<T> y22 = su2_low(p2, q2, x02, X.e[2][2]);
+  su2_pq(x11, y22, x12, y21, p3, q3);  // subgroup (1,2)
+  // S = S3 S2 S1; S1 = [[p1, q1, 0], [-q1*, p1*, 0], [0, 0, 1]]
+  const cplx<T> zero = cmk<T>(T(0), T(0));
+  const cplx<T> s0[3] = {cmul(p2, p1), cmul(p2, q1), q2};
+  const cplx<T> t2[3] = {cmul(cmk<T>(-q2.re, q2.im), p1), cmul(cmk<T>(-q2.re, q2.im), q1),
+                         cconj(p2)};
+  const cplx<T> r1[3] = {cmk<T>(-q1.re, q1.im), cconj(p1), zero};
+  Mat3<T> R;  // S - 1
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    R.e[0][j] = s0[j];
+    R.e[1][j] = su2_high(p3, q3, r1[j], t2[j]);
+    R.e[2][j] = su2_low(p3, q3, r1[j], t2[j]);
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) R.e[k][k].re -= T(1);
+  const T c2 = omega * (omega - T(1)) * T(0.5);
+#pragma unroll
+  for (int r = 0; r < 2; r++) {
+    cplx<T> M[3];  // w R + c2 R^2, row r
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const cplx<T> r2 = mul_entry(R, R, r, j);
+      M[j] = cmk<T>(fm(omega, R.e[r][j].re, c2 * r2.re), fm(omega, R.e[r][j].im, c2 * r2.im));
+    }
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      cplx<T> o = gold.e[r][j];
+#pragma unroll
+      for (int k = 0; k < 3; k++) cmac(o, M[k], gold.e[k][j]);
+      gn.e[r][j] = o;
+    }
+  }
+  normalize<T, false>(gn);
+}
+
+// ---------------------------------------------------------------------------
 // Field layout in HBM
 // ---------------------------------------------------------------------------
 // A field of n matrices per (parity, slot) is stored as NCHUNK planes of 16-byte

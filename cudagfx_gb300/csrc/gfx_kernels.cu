@@ -42,7 +42,7 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // MODE (launch_or_halfsweep's mode): 0 plain loads; 1 each block first issues one
 // L2 bulk prefetch per contiguous range it reads.
 template <typename T, int NRU, int NDIR, int MODE>
-__global__ void __launch_bounds__(256) or_halfsweep_kernel(Lattice L,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) or_halfsweep_kernel(Lattice L,
                                                             const typename VecOf<T>::type* U,
                                                             typename VecOf<T>::type* G, int parity,
                                                             T omega) {
@@ -54,18 +54,8 @@ __global__ void __launch_bounds__(256) or_halfsweep_kernel(Lattice L,
   }
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= L.vh) return;
-  const size_t vh = (size_t)L.vh;
   const Site c = site_of(L, i, parity);
-  Mat3<T> star;
-  compute_star<T, T, NRU, T, 12, NDIR>(L, c, parity, U, G, star);
-  typename VecOf<T>::type* Gp = G + (size_t)parity * NCG * vh;
-  Mat3<T> gold, g, gn;
-  Field<T, 12>::load(Gp, vh, i, gold);
-  g = gold;
-  cm_relax(g, star);
-  normalize<T, true>(g);
-  overrelax_rows01(gn, gold, g, omega);
-  Field<T, 12>::store(Gp, vh, i, gn);
+  or_site_update<T, NRU, NDIR>(L, c, parity, U, G, i, omega);
 }
 
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
