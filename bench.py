@@ -242,6 +242,7 @@ def synthetic_mt_params(seed=4172):
 
 # ---------------------------------------------------------------------------
 def dist_init(args):
+    """torchrun ranks: NCCL between GPUs, gloo when no GPU is present (tests)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0, None
@@ -249,26 +250,40 @@ def dist_init(args):
     import torch.distributed as dist
     rank = int(os.environ["RANK"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        dist.init_process_group("gloo")
     return rank, ws, local, dist
+
+
+def _coll_device():
+    import torch
+    return "cuda" if torch.cuda.is_available() else "cpu"
 
 
 def barrier(dist):
     if dist is not None:
         import torch
-        t = torch.zeros(1, device="cuda")
+        t = torch.zeros(1, device=_coll_device())
         dist.all_reduce(t)
-        torch.cuda.synchronize()
+        if t.is_cuda:
+            torch.cuda.synchronize()
 
 
 def max_over_ranks(dist, x):
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device=_coll_device())
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_inputs(rank):
+    """Each rank fixes its own configuration: heatbath seed and gauge-start seed."""
+    return {"mt_seed": 42 + rank, "trafo_seed": 351 + rank}
 
 
 def cpu_reference_rate(dims, sweeps, omega, seed=351):
@@ -353,14 +368,15 @@ def run_gfx(args, dims):
             c.mt_load_params(synthetic_mt_params())
 
     mt_source(ctx)
-    ctx.mt_seed(42 + rank)
+    seeds = replica_inputs(rank)
+    ctx.mt_seed(seeds["mt_seed"])
     ctx.mt_init(2 * V, 8 * V)
     t0 = time.perf_counter()
     ctx.thermalize(args.beta, args.therm, variant=gfx.HB_KENNEDY_PENDLETON)
     therm_s = time.perf_counter() - t0
     plaq = ctx.plaquette()
     links = ctx.get_links()
-    g0 = gfx.random_init_reference(351 + rank, V)
+    g0 = gfx.random_init_reference(seeds["trafo_seed"], V)
 
     def make_params(ck):
         return ctx.or_params(maxit=20000, eps=args.eps, checkinterval=ck, omega=args.omega,

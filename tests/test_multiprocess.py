@@ -1,0 +1,53 @@
+"""The replica path of bench.py at world size 2 on CPU (gloo): the rendezvous, the
+barrier, the max over ranks that times a step, and one configuration per rank."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _rank_main(rank, ws, port, out):
+    sys.path.insert(0, ROOT)
+    os.environ.update(RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE=str(ws),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import bench
+    r, w, local, dist = bench.dist_init(None)
+    assert (r, w, local) == (rank, ws, rank)
+    bench.barrier(dist)
+    t = bench.max_over_ranks(dist, 10.0 * (rank + 1))  # per-rank step times
+    seeds = bench.replica_inputs(rank)
+    import torch
+    gathered = [None] * ws
+    dist.all_gather_object(gathered, seeds)
+    out[rank] = (t, gathered)
+    dist.destroy_process_group()
+
+
+def test_two_replicas_gloo():
+    torch = pytest.importorskip("torch")
+    mp = torch.multiprocessing.get_context("spawn")
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        procs = [mp.Process(target=_rank_main, args=(r, 2, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(120)
+        assert all(p.exitcode == 0 for p in procs)
+        res = dict(out)
+    for rank in range(2):
+        t, seeds = res[rank]
+        assert t == 20.0  # the slowest rank's time is every rank's
+        assert seeds[0] != seeds[1]  # independent configurations
