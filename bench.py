@@ -63,6 +63,8 @@ def parse():
                     help="sweeps per check once theta < switch-eps (0: off)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
     ap.add_argument("--no-tune", action="store_true", help="library default launch settings")
+    ap.add_argument("--fp64-polish", action="store_true",
+                    help="polish with FP64 sweeps instead of double-float ones")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven check loop instead of the CUDA-graph while loop (same "
                          "kernels; profilers list each launch)")
@@ -383,6 +385,7 @@ def run_gfx(args, dims):
                              criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
                              checkinterval_double=args.checkinterval_double,
                              checkinterval_near=args.checkinterval_near,
+                             polish=0 if args.fp64_polish else 1,
                              use_graph=0 if args.no_graph else 1)
 
     def solve(c, p):
@@ -502,6 +505,7 @@ def run_gfx(args, dims):
             "checkinterval": params.checkinterval,
             "checkinterval_double": params.checkinterval_double,
             "checkinterval_near": params.checkinterval_near,
+            "polish": "FP64" if args.fp64_polish else "double-float (FP32 pairs), FP64-confirmed",
             "tuning": tune, "tuning_fp64": tune64,
             "parallelism": "replicas" if ws > 1 else "1 GPU",
             "l2": "inputs larger than L2 (FP32 links %d MB, FP64 links %d MB)"
@@ -509,7 +513,8 @@ def run_gfx(args, dims):
             "mt_params": "reference file" if dat else "synthetic stand-in",
             "plaquette": plaq, "therm_s": therm_s},
         "sweeps_per_solve": {"total": r_last.sweeps, "fp32": r_last.sweeps_single,
-                             "fp64": r_last.sweeps_double},
+                             "polish": r_last.sweeps_double,
+                             "polish_double_float": r_last.sweeps_polish_df},
         "time_to_theta_s": {"mixed": r_last.ms / 1000.0, "fp64": t_fp64,
                             "fp64_sweeps": sweeps64,
                             "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None},

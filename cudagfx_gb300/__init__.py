@@ -78,13 +78,15 @@ class ORParams(_c.Structure):
                 ("omega", _c.c_double), ("criterion", _c.c_int), ("gauge", _c.c_int),
                 ("switch_eps", _c.c_double), ("plateau_ratio", _c.c_double),
                 ("checkinterval_double", _c.c_int), ("use_graph", _c.c_int),
-                ("record_history", _c.c_int), ("checkinterval_near", _c.c_int)]
+                ("record_history", _c.c_int), ("checkinterval_near", _c.c_int),
+                ("polish", _c.c_int)]
 
 
 class ORResult(_c.Structure):
     _fields_ = [("iterations", _c.c_int), ("sweeps", _c.c_int), ("sweeps_single", _c.c_int),
                 ("sweeps_double", _c.c_int), ("converged", _c.c_int), ("checks", _c.c_int),
-                ("final_values", Functional), ("ms", _c.c_double)]
+                ("final_values", Functional), ("ms", _c.c_double),
+                ("sweeps_polish_df", _c.c_int)]
 
 
 class CheckRecord(_c.Structure):

@@ -34,13 +34,16 @@ struct gfx_ctx {
   int link_nr32;  // FP32 link copy: 12 or 8
   size_t u32_bytes;
   int block;
-  int or_block[2];  // OR/SA half-sweep block size, FP32 [0] and FP64 [1]
-  int or_pf[2];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
+  int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
+  int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
   double tune_sweep_ms[2], tune_measure_ms[2];
   int tune_ck;
   cudaStream_t stream;
   bool own_stream;
-  int g_active;  // 0: G32 holds the current g, 1: G64 does
+  int g_active;  // 0: G32 holds the current g, 1: G64 does, 2: Gdf does
+  void* Udf;     // double-float links (18 reals) and g (12 reals) of the polish sweeps
+  void* Gdf;
+  bool udf_valid;
   // fields
   void* U64;
   void* G64;
@@ -183,7 +186,7 @@ gfx_status gfx_destroy(gfx_ctx* ctx) {
   void* ptrs[] = {ctx->U64,     ctx->G64,  ctx->U32,  ctx->G32,  ctx->partials,
                   ctx->slice_sums, ctx->reduced, ctx->loop, ctx->hist, ctx->scratch_aos,
                   ctx->bank.a,  ctx->bank.b, ctx->bank.c, ctx->bank.seed, ctx->bank.status,
-                  ctx->gauss,   ctx->unif};
+                  ctx->gauss,   ctx->unif, ctx->Udf, ctx->Gdf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->loop_host) cudaFreeHost(ctx->loop_host);
@@ -220,8 +223,10 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->link_nr = link_reals64;
   ctx->link_nr32 = 12;
   ctx->block = 128;
-  ctx->or_block[0] = ctx->or_block[1] = 128;
-  ctx->or_pf[0] = ctx->or_pf[1] = 0;
+  ctx->or_block[0] = ctx->or_block[1] = ctx->or_block[2] = 128;
+  ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 0;
+  ctx->Udf = ctx->Gdf = nullptr;
+  ctx->udf_valid = false;
   ctx->tune_sweep_ms[0] = ctx->tune_sweep_ms[1] = 0.0;
   ctx->tune_measure_ms[0] = ctx->tune_measure_ms[1] = 0.0;
   ctx->tune_ck = 0;
@@ -338,7 +343,8 @@ gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
   if (s) return s;
   CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
   launch_pack_links(ctx->link_nr, ctx->L, ctx->scratch_aos, ctx->U64, ctx->stream);
-  if (ctx->U32) {
+  {
+    ctx->udf_valid = false;
     gfx_status rs = refresh_u32(ctx);
     if (rs) return rs;
   }
@@ -352,6 +358,24 @@ static gfx_status sync_g64(gfx_ctx* ctx) {
     launch_convert_g(0, 1, ctx->L, ctx->G32, ctx->G64, ctx->stream);
     CK(cudaGetLastError());
     ctx->g_active = 1;
+  } else if (ctx->g_active == 2) {
+    launch_convert_g_df(0, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);  // exact
+    CK(cudaGetLastError());
+    ctx->g_active = 1;
+  }
+  return GFX_OK;
+}
+
+// the double-float fields of the polish sweeps, allocated on first use; the links
+// are converted again after any change of the FP64 links
+static gfx_status ensure_df(gfx_ctx* ctx) {
+  gfx_status s;
+  if (!ctx->Udf && (s = dalloc(ctx, &ctx->Udf, (size_t)8 * 9 * 16 * (size_t)ctx->L.vh))) return s;
+  if (!ctx->Gdf && (s = dalloc(ctx, &ctx->Gdf, (size_t)2 * 6 * 16 * (size_t)ctx->L.vh))) return s;
+  if (!ctx->udf_valid) {
+    launch_convert_links_64_to_df(ctx->link_nr, ctx->L, ctx->U64, ctx->Udf, ctx->stream);
+    CK(cudaGetLastError());
+    ctx->udf_valid = true;
   }
   return GFX_OK;
 }
@@ -415,8 +439,23 @@ gfx_status gfx_unit_trafo(gfx_ctx* ctx) {
 // sweeps and measurements
 // ---------------------------------------------------------------------------
 static gfx_status prepare_g(gfx_ctx* ctx, int prec) {
+  if (prec == 2) {
+    gfx_status s = ensure_df(ctx);
+    if (s) return s;
+    if (ctx->g_active == 0 && (s = sync_g64(ctx))) return s;
+    if (ctx->g_active == 1) {
+      launch_convert_g_df(1, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);
+      CK(cudaGetLastError());
+      ctx->g_active = 2;
+    }
+    return GFX_OK;
+  }
   if (prec == 0) {
     if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "FP32 sweeps need a SINGLE or MIXED context");
+    if (ctx->g_active == 2) {
+      gfx_status s = sync_g64(ctx);
+      if (s) return s;
+    }
     if (ctx->g_active == 1) {
       launch_convert_g(1, 0, ctx->L, ctx->G64, ctx->G32, ctx->stream);
       CK(cudaGetLastError());
@@ -430,8 +469,8 @@ static gfx_status prepare_g(gfx_ctx* ctx, int prec) {
 }
 
 static void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
-  const void* U = prec == 0 ? ctx->U32 : ctx->U64;
-  void* G = prec == 0 ? ctx->G32 : ctx->G64;
+  const void* U = prec == 0 ? ctx->U32 : prec == 2 ? ctx->Udf : ctx->U64;
+  void* G = prec == 0 ? ctx->G32 : prec == 2 ? ctx->Gdf : ctx->G64;
   for (int p = 0; p < 2; p++)
     launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
                         ctx->or_pf[prec], ctx->stream);
@@ -451,8 +490,8 @@ static int meas_block(const gfx_ctx* ctx) {
 
 static void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
   const int b = meas_block(ctx);
-  const void* U = cprec == 0 ? ctx->U32 : ctx->U64;
-  const void* G = gprec == 0 ? ctx->G32 : ctx->G64;
+  const void* U = cprec == 0 ? ctx->U32 : cprec == 2 ? ctx->Udf : ctx->U64;
+  const void* G = gprec == 0 ? ctx->G32 : gprec == 2 ? ctx->Gdf : ctx->G64;
   launch_measure(cprec, lnr(ctx, cprec), gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
   ctx->launches += 1;
 }
@@ -469,7 +508,7 @@ static void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
 gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, int precision) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
   if (parity < 0 || parity > 1) return fail(ctx, GFX_ERR_ARG, "parity must be 0 or 1");
-  const int prec = precision == 0 ? 0 : 1;
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
@@ -483,7 +522,7 @@ gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, i
 
 gfx_status gfx_or_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
-  const int prec = precision == 0 ? 0 : 1;
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
@@ -498,8 +537,8 @@ gfx_status gfx_functional(gfx_ctx* ctx, int gauge, int precision, gfx_functional
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
   int cprec = precision == 0 ? 0 : 1;
   if (cprec == 0 && !ctx->U32) cprec = 1;
-  if (cprec == 0) {
-    gfx_status s = prepare_g(ctx, 0);
+  if (cprec == 0 || ctx->g_active == 2) {
+    gfx_status s = prepare_g(ctx, cprec);
     if (s) return s;
   }
   const int gprec = cprec == 0 ? 0 : ctx->g_active;
@@ -544,7 +583,8 @@ gfx_status gfx_apply_trafo(gfx_ctx* ctx) {
   gfx_status s = sync_g64(ctx);
   if (s) return s;
   launch_apply_trafo(ctx->link_nr, ctx->L, ctx->U64, ctx->G64, ctx->stream);
-  if (ctx->U32) {
+  {
+    ctx->udf_valid = false;
     gfx_status rs = refresh_u32(ctx);
     if (rs) return rs;
   }
@@ -676,7 +716,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   s = write_loop(ctx);
   if (s) return s;
 
-  int sweeps_single = 0, sweeps_double = 0;
+  int sweeps_single = 0, sweeps_double = 0, sweeps_df = 0;
   // iteration 0: sweep, then the first check (overrelax.cu:710-789)
   enqueue_sweeps(ctx, prec, ndir, p.omega, 1);
   (prec == 0 ? sweeps_single : sweeps_double)++;
@@ -708,6 +748,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
         }
       }
       (prec == 0 ? sweeps_single : sweeps_double) += H.iter - it0;
+      if (prec == 2) sweeps_df += H.iter - it0;
     }
     if (H.done == 4) {
       // below switch_eps: the same phase continues with the shorter interval
@@ -717,11 +758,29 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       if (s) return s;
       continue;
     }
-    if (H.done == 2) {
-      // FP32 phase finished: widen g (reunitarized in FP64) and verify in FP64
+    if (H.done == 1 && prec == 2) {
+      // the double-float polish reached eps: confirm with an FP64 measurement; if it
+      // does not, FP64 sweeps continue
       s = prepare_g(ctx, 1);
       if (s) return s;
       prec = 1;
+      H.done = 0;
+      s = write_loop(ctx);
+      if (s) return s;
+      enqueue_measure(ctx, 1, 1, ndir);
+      enqueue_reduce(ctx, ndir, true, 0, 0, 0);
+      CK(cudaGetLastError());
+      s = read_loop(ctx);
+      if (s) return s;
+      continue;
+    }
+    if (H.done == 2) {
+      // FP32 phase finished: widen g (reunitarized in FP64), then polish in FP64 or
+      // double-float; the first check verifies the handover state
+      s = prepare_g(ctx, 1);
+      if (s) return s;
+      prec = p.polish ? 2 : 1;
+      if (prec == 2 && (s = prepare_g(ctx, 2))) return s;
       H.phase = 1;
       H.done = 0;
       H.prev = 0.0;
@@ -729,7 +788,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       H.ck_near = 0;
       s = write_loop(ctx);
       if (s) return s;
-      enqueue_measure(ctx, 1, 1, ndir);
+      enqueue_measure(ctx, prec, prec, ndir);
       enqueue_reduce(ctx, ndir, true, 0, 0, 0);
       CK(cudaGetLastError());
       s = read_loop(ctx);
@@ -744,6 +803,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
     const int tail = p.maxit - 1 - H.iter;
     enqueue_sweeps(ctx, prec, ndir, p.omega, tail);
     (prec == 0 ? sweeps_single : sweeps_double) += tail > 0 ? tail : 0;
+    if (prec == 2) sweeps_df += tail > 0 ? tail : 0;
     if (prec == 0 && handover) {
       s = prepare_g(ctx, 1);
       if (s) return s;
@@ -775,6 +835,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
     res->sweeps_single = sweeps_single;
     res->sweeps_double = sweeps_double;
     res->sweeps = sweeps_single + sweeps_double;
+    res->sweeps_polish_df = sweeps_df;
     res->checks = H.nhist;
     res->final_values.F = H.last_F;
     res->final_values.dAdA = H.last_dAdA;
@@ -1054,7 +1115,8 @@ gfx_status gfx_link_heatbath_halfsweep(gfx_ctx* ctx, int parity, int nu, double 
     return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
   launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, parity, nu, beta / 3.0, ctx->gauss,
                        ctx->unif, variant, 128, ctx->stream);
-  if (ctx->U32) {
+  {
+    ctx->udf_valid = false;
     gfx_status rs = refresh_u32(ctx);
     if (rs) return rs;
   }
@@ -1087,7 +1149,8 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
       np++;
     }
   }
-  if (ctx->U32) {
+  {
+    ctx->udf_valid = false;
     gfx_status rs = refresh_u32(ctx);
     if (rs) return rs;
   }
@@ -1099,7 +1162,7 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
 gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision,
                            double* ms) {
   if (!ctx || !ms || nsweeps < 1) return fail(ctx, GFX_ERR_ARG, "gfx_time_sweeps: bad argument");
-  const int prec = precision == 0 ? 0 : 1;
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;

@@ -3,6 +3,8 @@
 // block reduction.  Sharing them keeps the batched results bit-identical per copy.
 #pragma once
 
+#include <type_traits>
+
 #include "gfx_device.cuh"
 #include "gfx_internal.h"
 
@@ -210,7 +212,8 @@ __device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c
 }
 
 // One overrelaxation site update (overrelax.cu:335-446) of site i of parity `parity`
-// in place: FP64 in the reference's operation order, FP32 with the reduced forms.
+// in place: FP64 in the reference's operation order; FP32 and double-float with the
+// reduced forms.
 template <typename T, int NRU, int NDIR>
 __device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, int parity,
                                                const typename VecOf<T>::type* __restrict__ U,
@@ -225,8 +228,8 @@ __device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, 
   else
     compute_star<T, T, NRU, T, 12, NDIR>(L, c, parity, U, G, star);
   Field<T, 12>::load(Gp, vh, i, gold);
-  if constexpr (sizeof(T) == 4) {
-    or_update_composed(gold, star, omega, gn);
+  if constexpr (!std::is_same<T, double>::value) {
+    or_update_composed(gold, star, omega, gn);  // FP32 and double-float
   } else {
     Mat3<T> g = gold;
     cm_relax(g, star);

@@ -13,6 +13,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "gfx_df.cuh"
+
 namespace gfx {
 
 // ---------------------------------------------------------------------------
@@ -47,6 +49,10 @@ __device__ __forceinline__ float fm<float>(float a, float b, float c) {
 template <>
 __device__ __forceinline__ double fm<double>(double a, double b, double c) {
   return __fma_rn(a, b, c);
+}
+template <>
+__device__ __forceinline__ dfl fm<dfl>(dfl a, dfl b, dfl c) {
+  return df_fma(a, b, c);
 }
 
 template <typename T>
@@ -98,6 +104,10 @@ __device__ __forceinline__ float rsqrt_t<float>(float x) {
 template <>
 __device__ __forceinline__ double rsqrt_t<double>(double x) {
   return rsqrt(x);
+}
+template <>
+__device__ __forceinline__ dfl rsqrt_t<dfl>(dfl x) {
+  return df_rsqrt(x);
 }
 
 template <typename T>
@@ -434,6 +444,11 @@ template <>
 struct VecOf<double> {
   typedef double2 type;
 };
+// a double-float complex number: (re.hi, re.lo, im.hi, im.lo)
+template <>
+struct VecOf<dfl> {
+  typedef float4 type;
+};
 
 template <typename T, int NR>
 struct Field {
@@ -576,6 +591,43 @@ __device__ __forceinline__ void Field<double, 18>::store(double2* __restrict__ b
                                                          const Mat3<double>& m) {
 #pragma unroll
   for (int k = 0; k < 9; k++) base[k * stride + i] = make_double2(m.e[k / 3][k % 3].re, m.e[k / 3][k % 3].im);
+}
+
+// double-float fields: one complex entry per 16-byte chunk, rows 0..1 (12 reals,
+// row 2 rebuilt) or rows 0..2 (18 reals)
+template <int NR>
+__device__ __forceinline__ void load_df(const float4* __restrict__ base, size_t stride, int i,
+                                        Mat3<dfl>& m) {
+#pragma unroll
+  for (int k = 0; k < NR / 2; k++) {
+    const float4 v = __ldg(base + k * stride + i);
+    m.e[k / 3][k % 3] = cmk<dfl>(dfl(v.x, v.y), dfl(v.z, v.w));
+  }
+  if (NR == 12) row2_from_01(m);
+}
+template <int NR>
+__device__ __forceinline__ void store_df(float4* __restrict__ base, size_t stride, int i,
+                                         const Mat3<dfl>& m) {
+#pragma unroll
+  for (int k = 0; k < NR / 2; k++) {
+    const cplx<dfl> z = m.e[k / 3][k % 3];
+    base[k * stride + i] = make_float4(z.re.hi, z.re.lo, z.im.hi, z.im.lo);
+  }
+}
+template <>
+__device__ __forceinline__ void Field<dfl, 12>::load(const float4* __restrict__ base, size_t stride,
+                                                     int i, Mat3<dfl>& m) {
+  load_df<12>(base, stride, i, m);
+}
+template <>
+__device__ __forceinline__ void Field<dfl, 12>::store(float4* __restrict__ base, size_t stride,
+                                                      int i, const Mat3<dfl>& m) {
+  store_df<12>(base, stride, i, m);
+}
+template <>
+__device__ __forceinline__ void Field<dfl, 18>::load(const float4* __restrict__ base, size_t stride,
+                                                     int i, Mat3<dfl>& m) {
+  load_df<18>(base, stride, i, m);
 }
 
 // ---------------------------------------------------------------------------

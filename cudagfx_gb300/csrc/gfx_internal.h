@@ -44,8 +44,9 @@ struct Reduced {
 };
 
 // ----- kernel launchers (gfx_kernels.cu) -----
+// prec: 0 FP32, 1 FP64, 2 double-float (links 18 reals, g 12 reals, float pairs).
 // link_nr arguments give the layout of the link field read: FP32 12 or 8 reals when
-// prec == 0, FP64 12 or 18 reals otherwise
+// prec == 0, FP64 12 or 18 reals when prec == 1
 // mode: 0 plain loads, 1 L2 bulk prefetch per block
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
                          int parity, double omega, int block, int mode, cudaStream_t s);
@@ -66,6 +67,10 @@ void launch_unpack_links(int link_nr_prec, const Lattice& L, const void* U, doub
                          cudaStream_t s);
 void launch_pack_g(int gprec, const Lattice& L, const double* aos, void* G, cudaStream_t s);
 void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cudaStream_t s);
+// double-float copies of the links (18 reals) and of g (12 reals; to_df = 0 back to FP64)
+void launch_convert_links_64_to_df(int link_nr, const Lattice& L, const void* U64, void* Udf,
+                                   cudaStream_t s);
+void launch_convert_g_df(int to_df, const Lattice& L, void* G64, void* Gdf, cudaStream_t s);
 // link_nr32: FP32 layout of the copy, 12 or 8 reals
 void launch_convert_links_64_to_32(int link_nr, int link_nr32, const Lattice& L, const void* U64,
                                    void* U32, cudaStream_t s);

@@ -42,7 +42,7 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // MODE (launch_or_halfsweep's mode): 0 plain loads; 1 each block first issues one
 // L2 bulk prefetch per contiguous range it reads.
 template <typename T, int NRU, int NDIR, int MODE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) or_halfsweep_kernel(Lattice L,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) or_halfsweep_kernel(Lattice L,
                                                             const typename VecOf<T>::type* U,
                                                             typename VecOf<T>::type* G, int parity,
                                                             T omega) {
@@ -70,7 +70,10 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
     else                                                                                         \
       or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
   } while (0)
-  if (prec == 0 && link_nr == 8) {
+  if (prec == 2) {  // double-float, 18-real links
+    if (ndir == 4) OR_LAUNCH(dfl, 18, 4);
+    else OR_LAUNCH(dfl, 18, 3);
+  } else if (prec == 0 && link_nr == 8) {
     if (ndir == 4) OR_LAUNCH(float, 8, 4);
     else OR_LAUNCH(float, 8, 3);
   } else if (prec == 0) {
@@ -125,7 +128,10 @@ void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& 
   measure_kernel<TC, TSU, NR, TSG, ND><<<grid, block, 0, s>>>(                      \
       L, (const typename VecOf<TSU>::type*)U, (const typename VecOf<TSG>::type*)G, \
       partials)
-  if (cprec == 0 && link_nr == 8) {
+  if (cprec == 2) {  // double-float, 18-real links, double-float g
+    if (ndir == 4) MEAS(dfl, dfl, 18, dfl, 4);
+    else MEAS(dfl, dfl, 18, dfl, 3);
+  } else if (cprec == 0 && link_nr == 8) {
     if (ndir == 4) MEAS(float, float, 8, float, 4);
     else MEAS(float, float, 8, float, 3);
   } else if (cprec == 0) {
@@ -489,6 +495,57 @@ void launch_convert_links_64_to_32(int link_nr, int link_nr32, const Lattice& L,
     if (link_nr32 == 8) links_64_to_32_kernel<12, 8><<<grid, 128, 0, s>>>(L, u, o);
     else links_64_to_32_kernel<12, 12><<<grid, 128, 0, s>>>(L, u, o);
   }
+}
+
+// double-float copies: links as 18 reals (rows 0..2), g as 12; hi = fl(d), lo = fl(d - hi)
+template <int NR>
+__global__ void links_64_to_df_kernel(Lattice L, const double2* U64, float4* Udf) {
+  const int blk = blockIdx.y;  // parity*4 + mu
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  Mat3<double> m;
+  Field<double, NR>::load(U64 + (size_t)blk * Field<double, NR>::NCHUNK * L.vh, (size_t)L.vh, i, m);
+  float4* o = Udf + (size_t)blk * 9 * L.vh;
+#pragma unroll
+  for (int k = 0; k < 9; k++) {
+    const dfl re(m.e[k / 3][k % 3].re), im(m.e[k / 3][k % 3].im);
+    o[(size_t)k * L.vh + i] = make_float4(re.hi, re.lo, im.hi, im.lo);
+  }
+}
+
+void launch_convert_links_64_to_df(int link_nr, const Lattice& L, const void* U64, void* Udf,
+                                   cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 8);
+  if (link_nr == 18)
+    links_64_to_df_kernel<18><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)Udf);
+  else
+    links_64_to_df_kernel<12><<<grid, 128, 0, s>>>(L, (const double2*)U64, (float4*)Udf);
+}
+
+// g: 12 reals per site, both parities; to_df = 1: G64 -> Gdf, 0: Gdf -> G64 (exact)
+__global__ void g_df_kernel(Lattice L, double2* G64, float4* Gdf, int to_df) {
+  const int parity = blockIdx.y;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  double2* g = G64 + (size_t)parity * 6 * L.vh;
+  float4* h = Gdf + (size_t)parity * 6 * L.vh;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const size_t o = (size_t)k * L.vh + i;
+    if (to_df) {
+      const double2 v = g[o];
+      const dfl re(v.x), im(v.y);
+      h[o] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    } else {
+      const float4 v = h[o];
+      g[o] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
+  }
+}
+
+void launch_convert_g_df(int to_df, const Lattice& L, void* G64, void* Gdf, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128, 2);
+  g_df_kernel<<<grid, 128, 0, s>>>(L, (double2*)G64, (float4*)Gdf, to_df);
 }
 
 // g precision change; widening reunitarizes in FP64

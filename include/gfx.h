@@ -75,6 +75,10 @@ typedef struct {
   int record_history;     /* keep every check (gfx_or_history) */
   int checkinterval_near; /* sweeps between checks once the value is below switch_eps
                              (0: checkinterval throughout, the reference schedule) */
+  int polish;             /* mixed: 0 = FP64 sweeps after the handover; 1 = double-float
+                             sweeps (pairs of floats, ~48 bits) on the FP32 units, whose
+                             result an FP64 measurement confirms (FP64 sweeps continue if
+                             it does not).  GB300 runs FP32 64x faster than FP64. */
 } gfx_or_params;
 
 typedef struct {
@@ -86,6 +90,7 @@ typedef struct {
   int checks;         /* functional evaluations */
   gfx_functional_t final_values; /* last evaluation (FP64 unless precision is SINGLE) */
   double ms;          /* device time of the whole call (CUDA events) */
+  int sweeps_polish_df; /* of sweeps_double, those run in double-float (polish = 1) */
 } gfx_or_result;
 
 typedef struct {
@@ -195,7 +200,8 @@ void gfx_or_params_default(gfx_or_params *p);
 gfx_status gfx_overrelax(gfx_ctx *ctx, const gfx_or_params *p, gfx_or_result *res);
 /* copy up to cap check records of the last gfx_overrelax call; returns the count */
 int gfx_or_history(const gfx_ctx *ctx, gfx_check_record *out, int cap);
-/* nsweeps plain OR sweeps (even then odd) without checks; precision 0 = FP32, 1 = FP64 */
+/* nsweeps plain OR sweeps (even then odd) without checks; precision 0 = FP32, 1 = FP64,
+ * 2 = double-float (the polish sweeps of gfx_or_params.polish = 1) */
 gfx_status gfx_or_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision);
 /* one OR half-sweep of one parity */
 gfx_status gfx_or_halfsweep(gfx_ctx *ctx, int parity, double omega, int gauge, int precision);
