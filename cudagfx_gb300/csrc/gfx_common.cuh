@@ -45,6 +45,8 @@ struct Load<double, float, 12> {
 // block's DRAM requests in flight at once; the regular loads then hit L2.  It is a
 // hint: the neighbours that wrap around the lattice fall outside the ranges and
 // are fetched by the regular loads, and every range is clamped to its plane.
+// A tuner candidate (staging = 1): on GB300 the extra L2 traffic makes the FP32
+// sweep slower, and the FP64 sweeps are compute-bound either way.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void l2_prefetch_range(const void* plane, int vh, int a, int b) {
   a = max(a, 0);

@@ -297,7 +297,10 @@ gfx_status gfx_batch_get_trafo(gfx_batch *b, int conf, int copy, double *su3_tra
 /* Haar-random start for every copy: copy k of configuration c (global index
  * copy_base(c) + k) uses seed + global index (same generator as gfx_random_trafo_haar) */
 gfx_status gfx_batch_random_haar(gfx_batch *b, uint64_t seed);
-/* fix every copy (one device loop for the whole batch); results[gfx_batch_copies()] */
+/* fix every copy (one device loop for the whole batch); results[gfx_batch_copies()].
+ * Every copy follows exactly the trajectory of gfx_overrelax on a single context with
+ * the same parameters, except that the batch uses checkinterval throughout
+ * (checkinterval_near is ignored) and polishes with FP64 sweeps (polish is ignored). */
 gfx_status gfx_batch_overrelax(gfx_batch *b, const gfx_or_params *p, gfx_copy_result *results,
                                double *ms);
 /* the converged copy of configuration conf with the largest functional */
