@@ -243,6 +243,28 @@ def synthetic_mt_params(seed=4172):
 
 
 # ---------------------------------------------------------------------------
+class nvtx_range:
+    """An NVTX range (named in profiler launch lists) when torch provides NVTX."""
+
+    def __init__(self, name):
+        self.name = name
+        self.nvtx = None
+
+    def __enter__(self):
+        try:
+            import torch
+            self.nvtx = torch.cuda.nvtx
+            self.nvtx.range_push(self.name)
+        except Exception:  # noqa: BLE001  (no NVTX: the range is only a label)
+            self.nvtx = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.nvtx is not None:
+            self.nvtx.range_pop()
+        return False
+
+
 def dist_init(args):
     """torchrun ranks: NCCL between GPUs, gloo when no GPU is present (tests)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -409,7 +431,7 @@ def run_gfx(args, dims):
     # ---- timed region: K solves, device time of each (CUDA events on the ctx stream)
     barrier(dist)
     launches0 = ctx.launch_count()
-    with ClockSampler(local) as clk:
+    with ClockSampler(local) as clk, nvtx_range("timed_solves"):
         results = [solve(ctx, params) for _ in range(args.steps)]
     launches = ctx.launch_count() - launches0
     ms_total = sum(r.ms for r in results)
