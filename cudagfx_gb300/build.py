@@ -27,6 +27,8 @@ UNITS = {
     "gfx_heatbath.cu": [],
     "gfx_mt.cu": ["-prec-sqrt=false", "-prec-div=false", "-ftz=false"],
     "gfx_api.cu": [],
+    "gfx_tune.cu": [],
+    "gfx_ctx_files.cu": [],
     "gfx_noalloc.cu": [],
     "gfx_batch.cu": [],
     "gfx_host.cpp": [],

@@ -1,10 +1,7 @@
-// gfx_api.cu -- contexts, buffers and drivers behind the gfx_* C ABI.
-//
-// One context = one lattice on the current device, with
-//   U64 : links, FP64, 12 or 18 reals, even/odd SoA (authoritative copy)
-//   G64 : gauge transformation, FP64, 12 reals
-//   U32, G32 : FP32 12-real copies for the single/mixed-precision sweeps
-// and the work buffers of the reductions, the convergence loop and the twister bank.
+// gfx_api.cu -- contexts behind the gfx_* C ABI: lifecycle and buffers, fields,
+// sweeps and measurements, the convergence loop (a CUDA-graph while loop), the
+// twister bank, annealing and thermalization.  The context itself and the helpers
+// shared with gfx_tune.cu and gfx_ctx_files.cu are in gfx_context.h.
 // Everything runs on the context's stream; host synchronisation happens only where
 // a result is returned to the caller.
 #include <algorithm>
@@ -18,130 +15,18 @@
 #include <vector>
 
 #include "../../include/gfx.h"
-#include "../../include/gfx_io.h"
-#include "../../include/lime.h"
+#include "gfx_context.h"
 #include "gfx_internal.h"
 #include "gfx_io_internal.h"
 
 using namespace gfx;
 
-struct gfx_ctx {
-  int lx, ly, lz, lt;
-  long long vol;
-  Lattice L;
-  int precision;
-  int link_nr;    // FP64 link storage: 12 or 18
-  int link_nr32;  // FP32 link copy: 12 or 8
-  size_t u32_bytes;
-  int block;
-  int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
-  int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
-  double tune_sweep_ms[2], tune_measure_ms[2];
-  int tune_ck;
-  cudaStream_t stream;
-  bool own_stream;
-  int g_active;  // 0: G32 holds the current g, 1: G64 does, 2: Gdf does
-  void* Udf;     // double-float links (18 reals) and g (12 reals) of the polish sweeps
-  void* Gdf;
-  bool udf_valid;
-  // fields
-  void* U64;
-  void* G64;
-  void* U32;
-  void* G32;
-  // reductions
-  double* partials;
-  int part_cap;  // doubles
-  double* slice_sums;
-  Reduced* reduced;
-  LoopState* loop;
-  CheckRecord* hist;
-  int hist_cap;
-  LoopState* loop_host;  // pinned
-  Reduced* reduced_host; // pinned
-  double* scratch_aos;   // device staging for host<->device layout conversion
-  size_t scratch_bytes;
-  // twister bank
-  MTBank bank;
-  bool mt_params;
-  bool mt_seeded;
-  bool mt_init;
-  int n_gauss, n_unif, nper_g, nper_u;
-  float* gauss;
-  float* unif;
-  uint32_t h_params[4 * kMTCount];
-  // graph cache for the convergence loop
-  struct GraphEntry {
-    int cprec, ndir, ck, gprec;
-    double omega;
-    cudaGraphExec_t exec;
-    cudaGraph_t graph;
-  };
-  std::vector<GraphEntry> graphs;
-  std::vector<CheckRecord> last_hist;
-  size_t dev_bytes;
-  unsigned long long launches;  // kernels enqueued by this context (graph bodies included)
-  std::string err;
-};
-
 static std::string g_global_err;
 
-#define CK(call)                                                                     \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) {                                                         \
-      return fail(ctx, GFX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-    }                                                                                \
-  } while (0)
 
-static gfx_status fail(gfx_ctx* ctx, gfx_status s, const std::string& msg) {
-  if (ctx) ctx->err = msg;
-  g_global_err = msg;
-  return s;
-}
 
-namespace gfx {
-void set_global_error(const std::string& msg) { g_global_err = msg; }
-}  // namespace gfx
 
-static gfx_status dalloc(gfx_ctx* ctx, void** p, size_t bytes) {
-  cudaError_t e = cudaMalloc(p, bytes);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    *p = nullptr;
-    return fail(ctx, e == cudaErrorMemoryAllocation ? GFX_ERR_OOM : GFX_ERR_CUDA,
-                std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
-  }
-  ctx->dev_bytes += bytes;
-  return GFX_OK;
-}
 
-static size_t link_bytes64(const gfx_ctx* c) {
-  return (size_t)8 * (c->link_nr / 2) * 16 * (size_t)c->L.vh;  // 8 blocks x chunks x 16 B
-}
-static size_t link_bytes32(const gfx_ctx* c) { return (size_t)8 * 3 * 16 * (size_t)c->L.vh; }
-static size_t g_bytes64(const gfx_ctx* c) { return (size_t)2 * 6 * 16 * (size_t)c->L.vh; }
-static size_t g_bytes32(const gfx_ctx* c) { return (size_t)2 * 3 * 16 * (size_t)c->L.vh; }
-// the layout of the link field that precision prec reads
-static int lnr(const gfx_ctx* c, int prec) { return prec == 0 ? c->link_nr32 : c->link_nr; }
-// FP32 links: 12 reals = 3 planes of 16 bytes; 8 reals = 2 planes + the 3 planes of
-// exact rows kept for the links the 8-parameter form declines
-static size_t link_bytes32_for(const gfx_ctx* c, int nr32) {
-  return (size_t)8 * (nr32 == 8 ? 5 : 3) * 16 * (size_t)c->L.vh;
-}
-
-static gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes) {
-  if (ctx->scratch_bytes >= bytes) return GFX_OK;
-  if (ctx->scratch_aos) {
-    cudaFree(ctx->scratch_aos);
-    ctx->dev_bytes -= ctx->scratch_bytes;
-    ctx->scratch_aos = nullptr;
-    ctx->scratch_bytes = 0;
-  }
-  gfx_status s = dalloc(ctx, (void**)&ctx->scratch_aos, bytes);
-  if (s == GFX_OK) ctx->scratch_bytes = bytes;
-  return s;
-}
 
 static gfx_status ensure_hist(gfx_ctx* ctx, int cap) {
   if (ctx->hist_cap >= cap) return GFX_OK;
@@ -156,13 +41,42 @@ static gfx_status ensure_hist(gfx_ctx* ctx, int cap) {
   return s;
 }
 
-extern "C" {
+namespace gfx {
 
-const char* gfx_last_error(const gfx_ctx* ctx) {
-  return ctx ? ctx->err.c_str() : g_global_err.c_str();
+gfx_status fail(gfx_ctx* ctx, gfx_status s, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  g_global_err = msg;
+  return s;
+}
+void set_global_error(const std::string& msg) { g_global_err = msg; }
+const std::string& global_error() { return g_global_err; }
+
+gfx_status dalloc(gfx_ctx* ctx, void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? GFX_ERR_OOM : GFX_ERR_CUDA,
+                std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+  }
+  ctx->dev_bytes += bytes;
+  return GFX_OK;
 }
 
-static void destroy_graphs(gfx_ctx* ctx) {
+gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes) {
+  if (ctx->scratch_bytes >= bytes) return GFX_OK;
+  if (ctx->scratch_aos) {
+    cudaFree(ctx->scratch_aos);
+    ctx->dev_bytes -= ctx->scratch_bytes;
+    ctx->scratch_aos = nullptr;
+    ctx->scratch_bytes = 0;
+  }
+  gfx_status s = dalloc(ctx, (void**)&ctx->scratch_aos, bytes);
+  if (s == GFX_OK) ctx->scratch_bytes = bytes;
+  return s;
+}
+
+void destroy_graphs(gfx_ctx* ctx) {
   for (auto& g : ctx->graphs) {
     cudaGraphExecDestroy(g.exec);
     cudaGraphDestroy(g.graph);
@@ -171,13 +85,179 @@ static void destroy_graphs(gfx_ctx* ctx) {
 }
 
 // the FP32 link copy from the FP64 links, in the current FP32 layout
-static gfx_status refresh_u32(gfx_ctx* ctx) {
+gfx_status refresh_u32(gfx_ctx* ctx) {
   if (!ctx->U32) return GFX_OK;
   launch_convert_links_64_to_32(ctx->link_nr, ctx->link_nr32, ctx->L, ctx->U64, ctx->U32,
                                 ctx->stream);
   CK(cudaGetLastError());
   return GFX_OK;
 }
+
+gfx_status sync_g64(gfx_ctx* ctx) {
+  if (ctx->g_active == 0) {
+    launch_convert_g(0, 1, ctx->L, ctx->G32, ctx->G64, ctx->stream);
+    CK(cudaGetLastError());
+    ctx->g_active = 1;
+  } else if (ctx->g_active == 2) {
+    launch_convert_g_df(0, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);  // exact
+    CK(cudaGetLastError());
+    ctx->g_active = 1;
+  }
+  return GFX_OK;
+}
+
+// the double-float fields of the polish sweeps, allocated on first use; the links
+// are converted again after any change of the FP64 links
+gfx_status ensure_df(gfx_ctx* ctx) {
+  gfx_status s;
+  if (!ctx->Udf && (s = dalloc(ctx, &ctx->Udf, (size_t)8 * 9 * 16 * (size_t)ctx->L.vh))) return s;
+  if (!ctx->Gdf && (s = dalloc(ctx, &ctx->Gdf, (size_t)2 * 6 * 16 * (size_t)ctx->L.vh))) return s;
+  if (!ctx->udf_valid) {
+    launch_convert_links_64_to_df(ctx->link_nr, ctx->L, ctx->U64, ctx->Udf, ctx->stream);
+    CK(cudaGetLastError());
+    ctx->udf_valid = true;
+  }
+  return GFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// sweeps and measurements
+// ---------------------------------------------------------------------------
+gfx_status prepare_g(gfx_ctx* ctx, int prec) {
+  if (prec == 2) {
+    gfx_status s = ensure_df(ctx);
+    if (s) return s;
+    if (ctx->g_active == 0 && (s = sync_g64(ctx))) return s;
+    if (ctx->g_active == 1) {
+      launch_convert_g_df(1, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);
+      CK(cudaGetLastError());
+      ctx->g_active = 2;
+    }
+    return GFX_OK;
+  }
+  if (prec == 0) {
+    if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "FP32 sweeps need a SINGLE or MIXED context");
+    if (ctx->g_active == 2) {
+      gfx_status s = sync_g64(ctx);
+      if (s) return s;
+    }
+    if (ctx->g_active == 1) {
+      launch_convert_g(1, 0, ctx->L, ctx->G64, ctx->G32, ctx->stream);
+      CK(cudaGetLastError());
+      ctx->g_active = 0;
+    }
+  } else {
+    gfx_status s = sync_g64(ctx);
+    if (s) return s;
+  }
+  return GFX_OK;
+}
+
+void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
+  const void* U = prec == 0 ? ctx->U32 : prec == 2 ? ctx->Udf : ctx->U64;
+  void* G = prec == 0 ? ctx->G32 : prec == 2 ? ctx->Gdf : ctx->G64;
+  for (int p = 0; p < 2; p++)
+    launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
+                        ctx->or_pf[prec], ctx->stream);
+  ctx->launches += 2;
+}
+
+void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n) {
+  for (int k = 0; k < n; k++) enqueue_sweep(ctx, prec, ndir, omega);
+}
+
+static int meas_block(const gfx_ctx* ctx) {
+  // a measurement block covers part of one time slice of one parity; the batched
+  // measurement uses the same 128-site grouping, so sums agree bit for bit
+  (void)ctx;
+  return 128;
+}
+
+void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
+  const int b = meas_block(ctx);
+  const void* U = cprec == 0 ? ctx->U32 : cprec == 2 ? ctx->Udf : ctx->U64;
+  const void* G = gprec == 0 ? ctx->G32 : gprec == 2 ? ctx->Gdf : ctx->G64;
+  launch_measure(cprec, lnr(ctx, cprec), gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
+  ctx->launches += 1;
+}
+
+void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
+                           unsigned long long handle, int use_handle) {
+  const int nbx = measure_blocks_x(ctx->L, meas_block(ctx));
+  launch_reduce(ctx->L, ndir, ctx->partials, nbx, ctx->slice_sums, ctx->reduced,
+                with_loop ? ctx->loop : nullptr, with_loop ? ctx->hist : nullptr, advance, handle,
+                use_handle, ctx->stream);
+  ctx->launches += 2;
+}
+
+// Re-pack the FP64 links as nr reals per link (12 or 18).  The new buffer is
+// allocated first, so a failed allocation leaves the context as it was.
+gfx_status relayout_links(gfx_ctx* ctx, int nr) {
+  if (nr == ctx->link_nr) return GFX_OK;
+  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  const size_t new_bytes = (size_t)8 * (nr / 2) * 16 * (size_t)ctx->L.vh;
+  void* nu = nullptr;
+  s = dalloc(ctx, &nu, new_bytes);
+  if (s) return s;
+  launch_unpack_links(ctx->link_nr, ctx->L, ctx->U64, ctx->scratch_aos, ctx->stream);
+  launch_pack_links(nr, ctx->L, ctx->scratch_aos, nu, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->U64);
+  ctx->dev_bytes -= link_bytes64(ctx);
+  ctx->U64 = nu;
+  ctx->link_nr = nr;
+  destroy_graphs(ctx);
+  return GFX_OK;
+}
+
+// FP32 link layout 12 or 8; the 8-real copy needs a larger buffer (allocated first)
+gfx_status set_link_layout32(gfx_ctx* ctx, int nr32) {
+  if (!ctx->U32 || nr32 == ctx->link_nr32) return GFX_OK;
+  const size_t need = link_bytes32_for(ctx, nr32);
+  if (need > ctx->u32_bytes) {
+    void* nu = nullptr;
+    gfx_status s = dalloc(ctx, &nu, need);
+    if (s) return s;
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->U32);
+    ctx->dev_bytes -= ctx->u32_bytes;
+    ctx->U32 = nu;
+    ctx->u32_bytes = need;
+  }
+  ctx->link_nr32 = nr32;
+  destroy_graphs(ctx);
+  gfx_status s = refresh_u32(ctx);
+  if (s) return s;
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+// the links of U64 (or of `src`, a device field of the same layout) as host AoS
+gfx_status links_to_host(gfx_ctx* ctx, const void* src, std::vector<double>& out) {
+  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
+  gfx_status s = ensure_scratch(ctx, bytes);
+  if (s) return s;
+  out.resize(18 * 4 * (size_t)ctx->vol);
+  launch_unpack_links(ctx->link_nr, ctx->L, src, ctx->scratch_aos, ctx->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out.data(), ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GFX_OK;
+}
+
+
+}  // namespace gfx
+
+extern "C" {
+
+const char* gfx_last_error(const gfx_ctx* ctx) {
+  return ctx ? ctx->err.c_str() : g_global_err.c_str();
+}
+
+
 
 gfx_status gfx_destroy(gfx_ctx* ctx) {
   if (!ctx) return GFX_OK;
@@ -353,32 +433,7 @@ gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
   return GFX_OK;
 }
 
-static gfx_status sync_g64(gfx_ctx* ctx) {
-  if (ctx->g_active == 0) {
-    launch_convert_g(0, 1, ctx->L, ctx->G32, ctx->G64, ctx->stream);
-    CK(cudaGetLastError());
-    ctx->g_active = 1;
-  } else if (ctx->g_active == 2) {
-    launch_convert_g_df(0, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);  // exact
-    CK(cudaGetLastError());
-    ctx->g_active = 1;
-  }
-  return GFX_OK;
-}
 
-// the double-float fields of the polish sweeps, allocated on first use; the links
-// are converted again after any change of the FP64 links
-static gfx_status ensure_df(gfx_ctx* ctx) {
-  gfx_status s;
-  if (!ctx->Udf && (s = dalloc(ctx, &ctx->Udf, (size_t)8 * 9 * 16 * (size_t)ctx->L.vh))) return s;
-  if (!ctx->Gdf && (s = dalloc(ctx, &ctx->Gdf, (size_t)2 * 6 * 16 * (size_t)ctx->L.vh))) return s;
-  if (!ctx->udf_valid) {
-    launch_convert_links_64_to_df(ctx->link_nr, ctx->L, ctx->U64, ctx->Udf, ctx->stream);
-    CK(cudaGetLastError());
-    ctx->udf_valid = true;
-  }
-  return GFX_OK;
-}
 
 gfx_status gfx_get_links(gfx_ctx* ctx, double* su3) {
   if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_get_links: NULL argument");
@@ -435,75 +490,11 @@ gfx_status gfx_unit_trafo(gfx_ctx* ctx) {
   return gfx_set_trafo(ctx, h.data());
 }
 
-// ---------------------------------------------------------------------------
-// sweeps and measurements
-// ---------------------------------------------------------------------------
-static gfx_status prepare_g(gfx_ctx* ctx, int prec) {
-  if (prec == 2) {
-    gfx_status s = ensure_df(ctx);
-    if (s) return s;
-    if (ctx->g_active == 0 && (s = sync_g64(ctx))) return s;
-    if (ctx->g_active == 1) {
-      launch_convert_g_df(1, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);
-      CK(cudaGetLastError());
-      ctx->g_active = 2;
-    }
-    return GFX_OK;
-  }
-  if (prec == 0) {
-    if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "FP32 sweeps need a SINGLE or MIXED context");
-    if (ctx->g_active == 2) {
-      gfx_status s = sync_g64(ctx);
-      if (s) return s;
-    }
-    if (ctx->g_active == 1) {
-      launch_convert_g(1, 0, ctx->L, ctx->G64, ctx->G32, ctx->stream);
-      CK(cudaGetLastError());
-      ctx->g_active = 0;
-    }
-  } else {
-    gfx_status s = sync_g64(ctx);
-    if (s) return s;
-  }
-  return GFX_OK;
-}
 
-static void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
-  const void* U = prec == 0 ? ctx->U32 : prec == 2 ? ctx->Udf : ctx->U64;
-  void* G = prec == 0 ? ctx->G32 : prec == 2 ? ctx->Gdf : ctx->G64;
-  for (int p = 0; p < 2; p++)
-    launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
-                        ctx->or_pf[prec], ctx->stream);
-  ctx->launches += 2;
-}
 
-static void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n) {
-  for (int k = 0; k < n; k++) enqueue_sweep(ctx, prec, ndir, omega);
-}
 
-static int meas_block(const gfx_ctx* ctx) {
-  // a measurement block covers part of one time slice of one parity; the batched
-  // measurement uses the same 128-site grouping, so sums agree bit for bit
-  (void)ctx;
-  return 128;
-}
 
-static void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
-  const int b = meas_block(ctx);
-  const void* U = cprec == 0 ? ctx->U32 : cprec == 2 ? ctx->Udf : ctx->U64;
-  const void* G = gprec == 0 ? ctx->G32 : gprec == 2 ? ctx->Gdf : ctx->G64;
-  launch_measure(cprec, lnr(ctx, cprec), gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
-  ctx->launches += 1;
-}
 
-static void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
-                           unsigned long long handle, int use_handle) {
-  const int nbx = measure_blocks_x(ctx->L, meas_block(ctx));
-  launch_reduce(ctx->L, ndir, ctx->partials, nbx, ctx->slice_sums, ctx->reduced,
-                with_loop ? ctx->loop : nullptr, with_loop ? ctx->hist : nullptr, advance, handle,
-                use_handle, ctx->stream);
-  ctx->launches += 2;
-}
 
 gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, int precision) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
@@ -1179,518 +1170,6 @@ gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, i
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   *ms = t;
-  return GFX_OK;
-}
-
-// ---------------------------------------------------------------------------
-// files around a context (include/gfx_io.h)
-// ---------------------------------------------------------------------------
-static gfx_status relayout_links(gfx_ctx* ctx, int nr);
-
-static void ctx_dims(const gfx_ctx* ctx, int d[4]) {
-  d[0] = ctx->lx;
-  d[1] = ctx->ly;
-  d[2] = ctx->lz;
-  d[3] = ctx->lt;
-}
-
-// the links of U64 (or of `src`, a device field of the same layout) as host AoS
-static gfx_status links_to_host(gfx_ctx* ctx, const void* src, std::vector<double>& out) {
-  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
-  gfx_status s = ensure_scratch(ctx, bytes);
-  if (s) return s;
-  out.resize(18 * 4 * (size_t)ctx->vol);
-  launch_unpack_links(ctx->link_nr, ctx->L, src, ctx->scratch_aos, ctx->stream);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(out.data(), ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  return GFX_OK;
-}
-
-gfx_status gfx_load_links_ildg(gfx_ctx* ctx, const char* path, gfx_ildg_info* info) {
-  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_load_links_ildg: NULL argument");
-  int d[4];
-  ctx_dims(ctx, d);
-  std::vector<double> links(18 * 4 * (size_t)ctx->vol);
-  gfx_status s = gfx_ildg_read(path, d, links.data(), info);
-  if (s) return fail(ctx, s, g_global_err);
-  return gfx_set_links(ctx, links.data());
-}
-
-gfx_status gfx_write_links_ildg(gfx_ctx* ctx, const char* path, int precision, double beta) {
-  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_write_links_ildg: NULL argument");
-  double plaq = 0.0;
-  gfx_status s = gfx_plaquette(ctx, &plaq);
-  if (s) return s;
-  std::vector<double> links;
-  if ((s = links_to_host(ctx, ctx->U64, links))) return s;
-  int d[4];
-  ctx_dims(ctx, d);
-  s = gfx_ildg_write(path, d, links.data(), precision, plaq, beta);
-  return s ? fail(ctx, s, g_global_err) : GFX_OK;
-}
-
-gfx_status gfx_write_fixed_ildg(gfx_ctx* ctx, const char* path, int precision, double beta) {
-  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_write_fixed_ildg: NULL argument");
-  gfx_status s = sync_g64(ctx);
-  if (s) return s;
-  // U' = g U g^+ in place, then the saved links back: the context is unchanged
-  void* saved = nullptr;
-  if ((s = dalloc(ctx, &saved, link_bytes64(ctx)))) return s;
-  CK(cudaMemcpyAsync(saved, ctx->U64, link_bytes64(ctx), cudaMemcpyDeviceToDevice, ctx->stream));
-  launch_apply_trafo(ctx->link_nr, ctx->L, ctx->U64, ctx->G64, ctx->stream);
-  double plaq = 0.0;
-  std::vector<double> links;
-  s = gfx_plaquette(ctx, &plaq);
-  if (s == GFX_OK) s = links_to_host(ctx, ctx->U64, links);
-  cudaMemcpyAsync(ctx->U64, saved, link_bytes64(ctx), cudaMemcpyDeviceToDevice, ctx->stream);
-  cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(saved);
-  ctx->dev_bytes -= link_bytes64(ctx);
-  if (s) return s;
-  if (e != cudaSuccess) return fail(ctx, GFX_ERR_CUDA, cudaGetErrorString(e));
-  int d[4];
-  ctx_dims(ctx, d);
-  s = gfx_ildg_write(path, d, links.data(), precision, plaq, beta);
-  return s ? fail(ctx, s, g_global_err) : GFX_OK;
-}
-
-// ---- checkpoints: LIME records of big-endian words ----
-namespace {
-struct CkptFile {
-  FILE* f = nullptr;
-  ~CkptFile() {
-    if (f) std::fclose(f);
-  }
-};
-int ckpt_record(LimeWriter* w, const char* type, const void* data, uint64_t n) {
-  LimeRecordHeader* h = limeCreateHeader(1, 1, (char*)type, n);
-  int st = limeWriteRecordHeader(h, w);
-  limeDestroyHeader(h);
-  if (st != LIME_SUCCESS || n == 0) return st;
-  n_uint64_t k = n;
-  return limeWriteRecordData((void*)data, &k, w);
-}
-}  // namespace
-
-gfx_status gfx_checkpoint_save(gfx_ctx* ctx, const char* path) {
-  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_checkpoint_save: NULL argument");
-  gfx_status s;
-  std::vector<double> links;
-  if ((s = links_to_host(ctx, ctx->U64, links))) return s;
-  // g: the FP64 field as host su3, plus the FP32 field as stored when it is the
-  // current one (the widening to FP64 reunitarizes, so both are kept)
-  const int active = ctx->g_active;
-  std::vector<float> g32;
-  if (active == 0) {
-    g32.resize(g_bytes32(ctx) / 4);
-    CK(cudaMemcpyAsync(g32.data(), ctx->G32, g_bytes32(ctx), cudaMemcpyDeviceToHost, ctx->stream));
-  }
-  std::vector<double> g(18 * (size_t)ctx->vol);
-  if ((s = gfx_get_trafo(ctx, g.data()))) return s;
-  ctx->g_active = active;  // gfx_get_trafo widened a current FP32 g; it stays current
-  char info[512];
-  std::snprintf(info, sizeof(info),
-                "gfx-checkpoint 1\ndims %d %d %d %d\nprecision %d\nlink_reals %d\ng_fp32 %d\n"
-                "mt_params %d\nmt_seeded %d\nmt_init %d\nn_gauss %d\nn_unif %d\n",
-                ctx->lx, ctx->ly, ctx->lz, ctx->lt, ctx->precision, ctx->link_nr, active == 0,
-                (int)ctx->mt_params, (int)ctx->mt_seeded, (int)ctx->mt_init, ctx->n_gauss,
-                ctx->n_unif);
-  CkptFile f;
-  if (!(f.f = std::fopen(path, "wb"))) return fail(ctx, GFX_ERR_IO, std::string("cannot create ") + path);
-  LimeWriter* w = limeCreateWriter(f.f);
-  int st = ckpt_record(w, "gfx-checkpoint-info", info, std::strlen(info));
-  to_be64(links.data(), links.size(), links.data());
-  if (st == LIME_SUCCESS) st = ckpt_record(w, "gfx-links", links.data(), 8 * links.size());
-  to_be64(g.data(), g.size(), g.data());
-  if (st == LIME_SUCCESS) st = ckpt_record(w, "gfx-trafo", g.data(), 8 * g.size());
-  if (st == LIME_SUCCESS && active == 0) {
-    to_be32(g32.data(), g32.size(), g32.data());
-    st = ckpt_record(w, "gfx-trafo-fp32", g32.data(), 4 * g32.size());
-  }
-  if (st == LIME_SUCCESS && ctx->mt_params) {
-    std::vector<uint32_t> p(ctx->h_params, ctx->h_params + 4 * kMTCount);
-    to_be32(p.data(), p.size(), p.data());
-    st = ckpt_record(w, "gfx-mt-params", p.data(), 4 * p.size());
-  }
-  if (st == LIME_SUCCESS && ctx->mt_init) {
-    std::vector<uint32_t> state((size_t)kMTN * kMTCount);
-    std::vector<float> ga((size_t)kMTCount * ctx->nper_g), un((size_t)kMTCount * ctx->nper_u);
-    if ((s = gfx_mt_read(ctx, ga.data(), un.data(), state.data(), nullptr))) {
-      limeDestroyWriter(w);
-      return s;
-    }
-    to_be32(state.data(), state.size(), state.data());
-    to_be32(ga.data(), ga.size(), ga.data());
-    to_be32(un.data(), un.size(), un.data());
-    st = ckpt_record(w, "gfx-mt-state", state.data(), 4 * state.size());
-    if (st == LIME_SUCCESS) st = ckpt_record(w, "gfx-mt-gauss", ga.data(), 4 * ga.size());
-    if (st == LIME_SUCCESS) st = ckpt_record(w, "gfx-mt-unif", un.data(), 4 * un.size());
-  }
-  const int st2 = limeDestroyWriter(w);
-  if (st != LIME_SUCCESS || st2 != LIME_SUCCESS || std::fflush(f.f) != 0)
-    return fail(ctx, GFX_ERR_IO, std::string("checkpoint write failed: ") + path);
-  return GFX_OK;
-}
-
-gfx_status gfx_checkpoint_load(gfx_ctx* ctx, const char* path) {
-  if (!ctx || !path) return fail(ctx, GFX_ERR_ARG, "gfx_checkpoint_load: NULL argument");
-  CkptFile f;
-  if (!(f.f = std::fopen(path, "rb"))) return fail(ctx, GFX_ERR_IO, std::string("cannot open ") + path);
-  LimeReader* r = limeCreateReader(f.f);
-  std::string info;
-  std::vector<unsigned char> links, g, g32, params, state, ga, un;
-  int st;
-  auto bad = [&](const std::string& why) {
-    limeDestroyReader(r);
-    return fail(ctx, GFX_ERR_IO, "checkpoint " + std::string(path) + ": " + why);
-  };
-  while ((st = limeReaderNextRecord(r)) == LIME_SUCCESS) {
-    const std::string type = limeReaderType(r);
-    std::vector<unsigned char>* dst = type == "gfx-links" ? &links
-                                      : type == "gfx-trafo" ? &g
-                                      : type == "gfx-trafo-fp32" ? &g32
-                                      : type == "gfx-mt-params" ? &params
-                                      : type == "gfx-mt-state" ? &state
-                                      : type == "gfx-mt-gauss" ? &ga
-                                      : type == "gfx-mt-unif" ? &un : nullptr;
-    const uint64_t n = limeReaderBytes(r);
-    if (type == "gfx-checkpoint-info") {
-      if (n > 4096) return bad("info record too long");
-      info.assign(n, '\0');
-      n_uint64_t k = n;
-      if (limeReaderReadData(&info[0], &k, r) != LIME_SUCCESS || k != n) return bad("truncated");
-    } else if (dst) {
-      dst->resize(n);
-      n_uint64_t k = n;
-      if (n && (limeReaderReadData(dst->data(), &k, r) != LIME_SUCCESS || k != n))
-        return bad("truncated " + type);
-    }
-  }
-  limeDestroyReader(r);
-  if (st != LIME_EOF) return fail(ctx, GFX_ERR_IO, std::string("checkpoint read error: ") + path);
-  int ver = 0, d[4] = {0, 0, 0, 0}, prec = -1, nr = 0, fp32 = 0, mp = 0, ms = 0, mi = 0, ng = 0,
-      nu = 0;
-  if (std::sscanf(info.c_str(),
-                  "gfx-checkpoint %d\ndims %d %d %d %d\nprecision %d\nlink_reals %d\ng_fp32 %d\n"
-                  "mt_params %d\nmt_seeded %d\nmt_init %d\nn_gauss %d\nn_unif %d",
-                  &ver, &d[0], &d[1], &d[2], &d[3], &prec, &nr, &fp32, &mp, &ms, &mi, &ng,
-                  &nu) != 13 ||
-      ver != 1)
-    return fail(ctx, GFX_ERR_IO, std::string("not a checkpoint: ") + path);
-  if (d[0] != ctx->lx || d[1] != ctx->ly || d[2] != ctx->lz || d[3] != ctx->lt)
-    return fail(ctx, GFX_ERR_IO, std::string("checkpoint of another lattice: ") + path);
-  const size_t nl = 18 * 4 * (size_t)ctx->vol, ng64 = 18 * (size_t)ctx->vol;
-  if (links.size() != 8 * nl || g.size() != 8 * ng64)
-    return fail(ctx, GFX_ERR_IO, std::string("checkpoint fields of the wrong size: ") + path);
-  if (fp32 && (!ctx->G32 || g32.size() != g_bytes32(ctx)))
-    return fail(ctx, GFX_ERR_IO, "checkpoint holds an FP32 g this context cannot take");
-  gfx_status s;
-  if (nr != ctx->link_nr && (s = relayout_links(ctx, nr))) return s;
-  from_be64(links.data(), nl, links.data());
-  if ((s = gfx_set_links(ctx, (const double*)links.data()))) return s;
-  from_be64(g.data(), ng64, g.data());
-  if ((s = gfx_set_trafo(ctx, (const double*)g.data()))) return s;
-  if (fp32) {
-    from_be32(g32.data(), g32.size() / 4, g32.data());
-    CK(cudaMemcpy(ctx->G32, g32.data(), g32.size(), cudaMemcpyHostToDevice));
-    ctx->g_active = 0;
-  }
-  if (mp) {
-    if (params.size() != 16 * (size_t)kMTCount) return fail(ctx, GFX_ERR_IO, "checkpoint: twister parameters");
-    from_be32(params.data(), 4 * kMTCount, params.data());
-    if ((s = gfx_mt_load_params(ctx, (const uint32_t*)params.data()))) return s;
-    ctx->mt_seeded = ms != 0;
-  }
-  if (mi) {
-    if ((s = gfx_mt_init(ctx, ng, nu))) return s;
-    if (state.size() != 4 * (size_t)kMTN * kMTCount || ga.size() != 4 * (size_t)kMTCount * ctx->nper_g ||
-        un.size() != 4 * (size_t)kMTCount * ctx->nper_u)
-      return fail(ctx, GFX_ERR_IO, "checkpoint: twister state of the wrong size");
-    from_be32(state.data(), state.size() / 4, state.data());
-    from_be32(ga.data(), ga.size() / 4, ga.data());
-    from_be32(un.data(), un.size() / 4, un.data());
-    CK(cudaMemcpy(ctx->bank.status, state.data(), state.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->gauss, ga.data(), ga.size(), cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->unif, un.data(), un.size(), cudaMemcpyHostToDevice));
-  }
-  return GFX_OK;
-}
-
-// ---------------------------------------------------------------------------
-// launch tuning
-// ---------------------------------------------------------------------------
-gfx_status gfx_get_tuning(const gfx_ctx* ctx, gfx_tuning* t) {
-  if (!ctx || !t) return fail(nullptr, GFX_ERR_ARG, "gfx_get_tuning: NULL argument");
-  for (int p = 0; p < 2; p++) {
-    t->block[p] = ctx->or_block[p];
-    t->staging[p] = ctx->or_pf[p];
-    t->sweep_ms[p] = ctx->tune_sweep_ms[p];
-    t->check_ms[p] = ctx->tune_measure_ms[p];
-  }
-  t->link_reals64 = ctx->link_nr;
-  t->link_reals32 = ctx->link_nr32;
-  t->checkinterval = ctx->tune_ck;
-  return GFX_OK;
-}
-
-// Re-pack the FP64 links as nr reals per link (12 or 18).  The new buffer is
-// allocated first, so a failed allocation leaves the context as it was.
-static gfx_status relayout_links(gfx_ctx* ctx, int nr) {
-  if (nr == ctx->link_nr) return GFX_OK;
-  const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
-  gfx_status s = ensure_scratch(ctx, bytes);
-  if (s) return s;
-  const size_t new_bytes = (size_t)8 * (nr / 2) * 16 * (size_t)ctx->L.vh;
-  void* nu = nullptr;
-  s = dalloc(ctx, &nu, new_bytes);
-  if (s) return s;
-  launch_unpack_links(ctx->link_nr, ctx->L, ctx->U64, ctx->scratch_aos, ctx->stream);
-  launch_pack_links(nr, ctx->L, ctx->scratch_aos, nu, ctx->stream);
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(ctx->stream));
-  cudaFree(ctx->U64);
-  ctx->dev_bytes -= link_bytes64(ctx);
-  ctx->U64 = nu;
-  ctx->link_nr = nr;
-  destroy_graphs(ctx);
-  return GFX_OK;
-}
-
-static bool valid_block(int b) { return b >= 32 && b <= 256 && b % 32 == 0; }
-
-// FP32 link layout 12 or 8; the 8-real copy needs a larger buffer (allocated first)
-static gfx_status set_link_layout32(gfx_ctx* ctx, int nr32) {
-  if (!ctx->U32 || nr32 == ctx->link_nr32) return GFX_OK;
-  const size_t need = link_bytes32_for(ctx, nr32);
-  if (need > ctx->u32_bytes) {
-    void* nu = nullptr;
-    gfx_status s = dalloc(ctx, &nu, need);
-    if (s) return s;
-    CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(ctx->U32);
-    ctx->dev_bytes -= ctx->u32_bytes;
-    ctx->U32 = nu;
-    ctx->u32_bytes = need;
-  }
-  ctx->link_nr32 = nr32;
-  destroy_graphs(ctx);
-  gfx_status s = refresh_u32(ctx);
-  if (s) return s;
-  CK(cudaStreamSynchronize(ctx->stream));
-  return GFX_OK;
-}
-
-gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
-  if (!ctx || !t) return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: NULL argument");
-  for (int p = 0; p < 2; p++) {
-    if (!valid_block(t->block[p]))
-      return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: block must be a multiple of 32 in [32, 256]");
-    if (t->staging[p] < 0 || t->staging[p] > 1)
-      return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: staging must be 0 or 1");
-  }
-  if (t->link_reals64 != 0 && t->link_reals64 != 12 && t->link_reals64 != 18)
-    return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals64 must be 0, 12 or 18");
-  if (t->checkinterval < 0) return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: checkinterval < 0");
-  if (t->link_reals32 != 0 && t->link_reals32 != 12 && t->link_reals32 != 8)
-    return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals32 must be 0, 12 or 8");
-  if (t->link_reals64) {
-    gfx_status s = relayout_links(ctx, t->link_reals64);
-    if (s) return s;
-  }
-  if (t->link_reals32 && t->link_reals32 != ctx->link_nr32 && ctx->U32) {
-    gfx_status s = set_link_layout32(ctx, t->link_reals32);
-    if (s) return s;
-  }
-  for (int p = 0; p < 2; p++) {
-    ctx->or_block[p] = t->block[p];
-    ctx->or_pf[p] = t->staging[p];
-  }
-  ctx->tune_ck = t->checkinterval;
-  destroy_graphs(ctx);
-  return GFX_OK;
-}
-
-// device time of n repetitions of enqueue(), after one untimed repetition
-static gfx_status time_reps(gfx_ctx* ctx, int n, const std::function<void()>& enqueue,
-                            double* ms) {
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
-  enqueue();
-  CK(cudaEventRecord(e0, ctx->stream));
-  for (int k = 0; k < n; k++) enqueue();
-  CK(cudaEventRecord(e1, ctx->stream));
-  CK(cudaEventSynchronize(e1));
-  float t = 0.f;
-  CK(cudaEventElapsedTime(&t, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  CK(cudaGetLastError());
-  *ms = t / n;
-  return GFX_OK;
-}
-
-static std::string tune_key(const gfx_ctx* ctx, int ndir) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
-    cudaGetLastError();
-    std::snprintf(prop.name, sizeof(prop.name), "unknown");
-    prop.multiProcessorCount = 0;
-  }
-  char key[512];
-  std::snprintf(key, sizeof(key), "%s|%d|%dx%dx%dx%d|prec%d|ndir%d", prop.name,
-                prop.multiProcessorCount, ctx->lx, ctx->ly, ctx->lz, ctx->lt, ctx->precision, ndir);
-  for (char* c = key; *c; c++)
-    if (*c == '\t' || *c == '\n') *c = ' ';
-  return key;
-}
-
-// cache line: key TAB block0 staging0 block1 staging1 link_reals64 link_reals32 sweep_ms0
-// sweep_ms1 check_ms0 check_ms1
-static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t) {
-  FILE* f = std::fopen(path, "r");
-  if (!f) return false;
-  char line[1024];
-  bool hit = false;
-  while (std::fgets(line, sizeof(line), f)) {
-    char* tab = std::strchr(line, '\t');
-    if (!tab || std::string(line, tab - line) != key) continue;
-    gfx_tuning c;
-    std::memset(&c, 0, sizeof(c));
-    if (std::sscanf(tab + 1, "%d %d %d %d %d %d %lf %lf %lf %lf", &c.block[0], &c.staging[0],
-                    &c.block[1], &c.staging[1], &c.link_reals64, &c.link_reals32, &c.sweep_ms[0],
-                    &c.sweep_ms[1], &c.check_ms[0], &c.check_ms[1]) == 10 &&
-        (c.link_reals32 == 12 || c.link_reals32 == 8) &&
-        valid_block(c.block[0]) && valid_block(c.block[1]) &&
-        (c.link_reals64 == 12 || c.link_reals64 == 18)) {
-      *t = c;  // the last valid line for a key wins
-      hit = true;
-    }
-  }
-  std::fclose(f);
-  return hit;
-}
-
-static void cache_append(const char* path, const std::string& key, const gfx_tuning& t) {
-  FILE* f = std::fopen(path, "a");
-  if (!f) return;  // the cache is an optimisation; an unwritable path only costs a re-tune
-  std::fprintf(f, "%s\t%d %d %d %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), t.block[0],
-               t.staging[0], t.block[1], t.staging[1], t.link_reals64, t.link_reals32,
-               t.sweep_ms[0], t.sweep_ms[1], t.check_ms[0], t.check_ms[1]);
-  std::fclose(f);
-}
-
-static int suggest_checkinterval(const gfx_ctx* ctx, int expected_sweeps) {
-  const int p = ctx->G32 ? 0 : 1;
-  if (expected_sweeps <= 0 || ctx->tune_sweep_ms[p] <= 0.0) return 0;
-  // checks every k sweeps cost (n/k) c; stopping at the first check past
-  // convergence wastes k/2 sweeps s on average: k* = sqrt(2 n c / s)
-  const double k = std::sqrt(2.0 * expected_sweeps * ctx->tune_measure_ms[p] / ctx->tune_sweep_ms[p]);
-  return std::min(100, std::max(5, (int)std::lround(k)));
-}
-
-gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char* cache_path,
-                        gfx_tuning* out) {
-  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
-  const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
-  const std::string key = tune_key(ctx, ndir);
-  gfx_tuning t;
-  gfx_status s;
-  if (cache_path && cache_lookup(cache_path, key, &t)) {
-    s = gfx_set_tuning(ctx, &t);
-    if (s) return s;
-    for (int p = 0; p < 2; p++) {
-      ctx->tune_sweep_ms[p] = t.sweep_ms[p];
-      ctx->tune_measure_ms[p] = t.check_ms[p];
-    }
-    ctx->tune_ck = suggest_checkinterval(ctx, expected_sweeps);
-    return out ? gfx_get_tuning(ctx, out) : GFX_OK;
-  }
-  // keep the current g: the candidate sweeps run on it
-  const int active = ctx->g_active;
-  void* gsrc = active ? ctx->G64 : ctx->G32;
-  const size_t gbytes = active ? g_bytes64(ctx) : g_bytes32(ctx);
-  void* saved = nullptr;
-  if (cudaMalloc(&saved, gbytes) != cudaSuccess) {
-    cudaGetLastError();
-    return fail(ctx, GFX_ERR_OOM, "gfx_autotune: no room to keep g during tuning");
-  }
-  if (cudaMemcpyAsync(saved, gsrc, gbytes, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess) {
-    cudaGetLastError();
-    cudaFree(saved);
-    return fail(ctx, GFX_ERR_CUDA, "gfx_autotune: copy of g failed");
-  }
-  const int blocks[4] = {64, 128, 192, 256};
-  s = GFX_OK;
-  for (int prec = 0; prec < 2 && s == GFX_OK; prec++) {
-    if (prec == 0 && !ctx->G32) continue;
-    if (prec == 1 && ctx->precision == GFX_PREC_SINGLE) continue;  // FP64 sweeps never run
-    // link layouts: FP64 12/18 reals, FP32 12/8 reals
-    int layouts[2] = {ctx->link_nr, ctx->link_nr == 12 ? 18 : 12};
-    const int nlayouts = 2;
-    if (prec == 0) {
-      layouts[0] = 12;
-      layouts[1] = 8;
-    }
-    double best = 1e30;
-    int bb = ctx->or_block[prec], bp = ctx->or_pf[prec], bnr = layouts[0];
-    int n = 0;
-    for (int li = 0; li < nlayouts && s == GFX_OK; li++) {
-      if (prec == 1 && (s = relayout_links(ctx, layouts[li]))) break;
-      if (prec == 0 && (s = set_link_layout32(ctx, layouts[li]))) break;
-      if ((s = prepare_g(ctx, prec))) break;
-      if (n == 0) {
-        double t1 = 0.0;
-        if ((s = time_reps(ctx, 2, [&]() { enqueue_sweep(ctx, prec, ndir, 1.7); }, &t1))) break;
-        n = std::min(40, std::max(2, (int)std::ceil(3.0 / std::max(t1, 1e-3))));
-      }
-      auto sweep = [&]() { enqueue_sweeps(ctx, prec, ndir, 1.7, n); };
-      const int nmodes = 2;
-      for (int round = 0; round < 2 && s == GFX_OK; round++)
-        for (int bi = 0; bi < 4 && s == GFX_OK; bi++)
-          for (int pf = 0; pf < nmodes && s == GFX_OK; pf++) {
-            ctx->or_block[prec] = blocks[bi];
-            ctx->or_pf[prec] = pf;
-            double ms = 0.0;
-            s = time_reps(ctx, 2, sweep, &ms);
-            ms /= n;
-            if (s == GFX_OK && ms < best) {
-              best = ms;
-              bb = blocks[bi];
-              bp = pf;
-              bnr = layouts[li];
-            }
-          }
-    }
-    if (s) break;
-    ctx->or_block[prec] = bb;
-    ctx->or_pf[prec] = bp;
-    if (prec == 1 && (s = relayout_links(ctx, bnr))) break;
-    if (prec == 0 && (s = set_link_layout32(ctx, bnr))) break;
-    ctx->tune_sweep_ms[prec] = best;
-    if ((s = prepare_g(ctx, prec))) break;
-    auto check = [&]() {
-      enqueue_measure(ctx, prec, prec, ndir);
-      enqueue_reduce(ctx, ndir, false, 0, 0, 0);
-    };
-    s = time_reps(ctx, std::max(2, n), check, &ctx->tune_measure_ms[prec]);
-  }
-  // put g back where it was
-  cudaError_t e = cudaMemcpyAsync(gsrc, saved, gbytes, cudaMemcpyDeviceToDevice, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(saved);
-  ctx->g_active = active;
-  destroy_graphs(ctx);
-  if (s) return s;
-  if (e != cudaSuccess) return fail(ctx, GFX_ERR_CUDA, std::string("gfx_autotune: ") + cudaGetErrorString(e));
-  ctx->tune_ck = suggest_checkinterval(ctx, expected_sweeps);
-  gfx_tuning res;
-  gfx_get_tuning(ctx, &res);
-  if (cache_path) cache_append(cache_path, key, res);
-  if (out) *out = res;
   return GFX_OK;
 }
 

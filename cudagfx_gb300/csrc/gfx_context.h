@@ -1,0 +1,133 @@
+// gfx_context.h -- the context behind a gfx_ctx handle and the helpers that the
+// context's translation units share (gfx_api.cu: lifecycle, fields, sweeps and the
+// solve loop; gfx_tune.cu: launch tuning; gfx_ctx_files.cu: files and checkpoints).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "../../include/gfx.h"
+#include "gfx_internal.h"
+
+// One context = one lattice on the current device, with
+//   U64 : links, FP64, 12 or 18 reals, even/odd SoA (authoritative copy)
+//   G64 : gauge transformation, FP64, 12 reals
+//   U32, G32 : FP32 copies for the single/mixed-precision sweeps (links 12 or 8 reals)
+//   Udf, Gdf : double-float copies for the polish sweeps
+// and the work buffers of the reductions, the convergence loop and the twister bank.
+struct gfx_ctx {
+  int lx, ly, lz, lt;
+  long long vol;
+  gfx::Lattice L;
+  int precision;
+  int link_nr;    // FP64 link storage: 12 or 18
+  int link_nr32;  // FP32 link copy: 12 or 8
+  size_t u32_bytes;
+  int block;
+  int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
+  int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
+  double tune_sweep_ms[2], tune_measure_ms[2];
+  int tune_ck;
+  cudaStream_t stream;
+  bool own_stream;
+  int g_active;  // 0: G32 holds the current g, 1: G64 does, 2: Gdf does
+  void* Udf;     // double-float links (18 reals) and g (12 reals) of the polish sweeps
+  void* Gdf;
+  bool udf_valid;
+  // fields
+  void* U64;
+  void* G64;
+  void* U32;
+  void* G32;
+  // reductions
+  double* partials;
+  int part_cap;  // doubles
+  double* slice_sums;
+  gfx::Reduced* reduced;
+  gfx::LoopState* loop;
+  gfx::CheckRecord* hist;
+  int hist_cap;
+  gfx::LoopState* loop_host;  // pinned
+  gfx::Reduced* reduced_host; // pinned
+  double* scratch_aos;   // device staging for host<->device layout conversion
+  size_t scratch_bytes;
+  // twister bank
+  gfx::MTBank bank;
+  bool mt_params;
+  bool mt_seeded;
+  bool mt_init;
+  int n_gauss, n_unif, nper_g, nper_u;
+  float* gauss;
+  float* unif;
+  uint32_t h_params[4 * gfx::kMTCount];
+  // graph cache for the convergence loop
+  struct GraphEntry {
+    int cprec, ndir, ck, gprec;
+    double omega;
+    cudaGraphExec_t exec;
+    cudaGraph_t graph;
+  };
+  std::vector<GraphEntry> graphs;
+  std::vector<gfx::CheckRecord> last_hist;
+  size_t dev_bytes;
+  unsigned long long launches;  // kernels enqueued by this context (graph bodies included)
+  std::string err;
+};
+
+// return a CUDA failure as GFX_ERR_CUDA from a function with a `ctx` in scope
+#define CK(call)                                                                     \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      return fail(ctx, GFX_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    }                                                                                \
+  } while (0)
+
+namespace gfx {
+
+// record msg as the context's and the library's last error; returns s
+gfx_status fail(gfx_ctx* ctx, gfx_status s, const std::string& msg);
+const std::string& global_error();
+
+// buffer sizes (8 link blocks or 2 g parities x 16-byte planes x Vh)
+inline size_t link_bytes64(const gfx_ctx* c) { return (size_t)8 * (c->link_nr / 2) * 16 * (size_t)c->L.vh; }
+inline size_t link_bytes32(const gfx_ctx* c) { return (size_t)8 * 3 * 16 * (size_t)c->L.vh; }
+inline size_t g_bytes64(const gfx_ctx* c) { return (size_t)2 * 6 * 16 * (size_t)c->L.vh; }
+inline size_t g_bytes32(const gfx_ctx* c) { return (size_t)2 * 3 * 16 * (size_t)c->L.vh; }
+// FP32 links: 12 reals = 3 planes; 8 reals = 2 planes + the 3 planes of exact rows
+// kept for the links the 8-parameter form declines
+inline size_t link_bytes32_for(const gfx_ctx* c, int nr32) {
+  return (size_t)8 * (nr32 == 8 ? 5 : 3) * 16 * (size_t)c->L.vh;
+}
+// the layout of the link field that precision prec (0 FP32, 1 FP64) reads
+inline int lnr(const gfx_ctx* c, int prec) { return prec == 0 ? c->link_nr32 : c->link_nr; }
+inline void ctx_dims(const gfx_ctx* ctx, int d[4]) {
+  d[0] = ctx->lx;
+  d[1] = ctx->ly;
+  d[2] = ctx->lz;
+  d[3] = ctx->lt;
+}
+
+gfx_status dalloc(gfx_ctx* ctx, void** p, size_t bytes);
+gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes);
+void destroy_graphs(gfx_ctx* ctx);
+// the FP32 link copy from the FP64 links, in the current FP32 layout
+gfx_status refresh_u32(gfx_ctx* ctx);
+// make G64 the current g (from G32 or Gdf)
+gfx_status sync_g64(gfx_ctx* ctx);
+gfx_status ensure_df(gfx_ctx* ctx);
+// make the g of precision prec (0 FP32, 1 FP64, 2 double-float) the current one
+gfx_status prepare_g(gfx_ctx* ctx, int prec);
+void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega);
+void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
+void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir);
+void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
+                    unsigned long long handle, int use_handle);
+// re-pack the FP64 links as nr reals per link (12 or 18)
+gfx_status relayout_links(gfx_ctx* ctx, int nr);
+// FP32 link layout 12 or 8
+gfx_status set_link_layout32(gfx_ctx* ctx, int nr32);
+// the links of U64 (or of src, a device field in U64's layout) as host su3
+gfx_status links_to_host(gfx_ctx* ctx, const void* src, std::vector<double>& out);
+
+}  // namespace gfx
