@@ -2,9 +2,10 @@
 """Benchmark: Landau gauge fixing of a 32^4 SU(3) lattice on one GB300.
 
 One step = one complete gauge-fixing solve: the mixed-precision checkerboard
-overrelaxation (FP32 12-real sweeps with FP64-accumulated checks, then FP64
-polish sweeps) from the same random gauge start until theta = (1/3V) sum tr[DD^+]
-< 1e-12, verified in FP64.  The links (beta = 6.0, heatbath-thermalized on the GPU
+overrelaxation (FP32 12-real sweeps with FP64-accumulated checks, then polish
+sweeps -- by default rebased FP32 sweeps, g = (1 + a) g_c with only the small a in
+FP32) from the same random gauge start until theta = (1/3V) sum tr[DD^+] < 1e-12,
+verified in FP64.  The links (beta = 6.0, heatbath-thermalized on the GPU
 from a cold start) and the starting transformation are generated once before the
 timed region.
 
@@ -44,6 +45,10 @@ FLOP_PER_UPDATE = 4766  # the reference's count (overrelax.cu:897)
 NCU_TRAFFIC_FP32 = {(32, 32, 32, 32): 254.05e6 + 15.68e6}
 
 
+POLISH_NAMES = {0: "FP64", 1: "double-float (FP32 pairs), FP64-confirmed",
+                2: "rebased FP32 (g = (1 + a) g_c, a in FP32), FP64-confirmed"}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -63,8 +68,8 @@ def parse():
                     help="sweeps per check once theta < switch-eps (0: off)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the all-FP64 comparison")
     ap.add_argument("--no-tune", action="store_true", help="library default launch settings")
-    ap.add_argument("--fp64-polish", action="store_true",
-                    help="polish with FP64 sweeps instead of double-float ones")
+    ap.add_argument("--polish", type=int, default=2, choices=[0, 1, 2],
+                    help="sweeps after the FP32 phase: 0 FP64, 1 double-float, 2 rebased FP32")
     ap.add_argument("--no-graph", action="store_true",
                     help="host-driven check loop instead of the CUDA-graph while loop (same "
                          "kernels; profilers list each launch)")
@@ -407,7 +412,7 @@ def run_gfx(args, dims):
                              criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
                              checkinterval_double=args.checkinterval_double,
                              checkinterval_near=args.checkinterval_near,
-                             polish=0 if args.fp64_polish else 1,
+                             polish=args.polish,
                              use_graph=0 if args.no_graph else 1)
 
     def solve(c, p):
@@ -527,7 +532,7 @@ def run_gfx(args, dims):
             "checkinterval": params.checkinterval,
             "checkinterval_double": params.checkinterval_double,
             "checkinterval_near": params.checkinterval_near,
-            "polish": "FP64" if args.fp64_polish else "double-float (FP32 pairs), FP64-confirmed",
+            "polish": POLISH_NAMES[args.polish],
             "tuning": tune, "tuning_fp64": tune64,
             "parallelism": "replicas" if ws > 1 else "1 GPU",
             "l2": "inputs larger than L2 (FP32 links %d MB, FP64 links %d MB)"
@@ -536,7 +541,8 @@ def run_gfx(args, dims):
             "plaquette": plaq, "therm_s": therm_s},
         "sweeps_per_solve": {"total": r_last.sweeps, "fp32": r_last.sweeps_single,
                              "polish": r_last.sweeps_double,
-                             "polish_double_float": r_last.sweeps_polish_df},
+                             "polish_double_float": r_last.sweeps_polish_df,
+                             "polish_rebased_fp32": r_last.sweeps_polish_fp32},
         "time_to_theta_s": {"mixed": r_last.ms / 1000.0, "fp64": t_fp64,
                             "fp64_sweeps": sweeps64,
                             "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None},

@@ -86,7 +86,7 @@ class ORResult(_c.Structure):
     _fields_ = [("iterations", _c.c_int), ("sweeps", _c.c_int), ("sweeps_single", _c.c_int),
                 ("sweeps_double", _c.c_int), ("converged", _c.c_int), ("checks", _c.c_int),
                 ("final_values", Functional), ("ms", _c.c_double),
-                ("sweeps_polish_df", _c.c_int)]
+                ("sweeps_polish_df", _c.c_int), ("sweeps_polish_fp32", _c.c_int)]
 
 
 class CheckRecord(_c.Structure):

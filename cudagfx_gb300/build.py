@@ -31,6 +31,7 @@ UNITS = {
     "gfx_ctx_files.cu": [],
     "gfx_noalloc.cu": [],
     "gfx_batch.cu": [],
+    "gfx_rebased.cu": [],
     "gfx_host.cpp": [],
     "gfx_legacy.cpp": [],
     "gfx_lime.cpp": [],

@@ -86,6 +86,7 @@ void destroy_graphs(gfx_ctx* ctx) {
 
 // the FP32 link copy from the FP64 links, in the current FP32 layout
 gfx_status refresh_u32(gfx_ctx* ctx) {
+  ctx->rb_valid = false;  // the rebased links follow the FP64 links too
   if (!ctx->U32) return GFX_OK;
   launch_convert_links_64_to_32(ctx->link_nr, ctx->link_nr32, ctx->L, ctx->U64, ctx->U32,
                                 ctx->stream);
@@ -102,8 +103,36 @@ gfx_status sync_g64(gfx_ctx* ctx) {
     launch_convert_g_df(0, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);  // exact
     CK(cudaGetLastError());
     ctx->g_active = 1;
+  } else if (ctx->g_active == 3) {
+    launch_compose_g(ctx->L, ctx->G64, ctx->G32, ctx->stream);  // g = (1 + a) g_c
+    CK(cudaGetLastError());
+    ctx->g_active = 1;
   }
   return GFX_OK;
+}
+
+// A new base: g_c = the current g (FP64), the rebased links and the split star from
+// it, a = 0.  The links' FP32 remainders pass through the scratch buffer.
+gfx_status rebase(gfx_ctx* ctx, int ndir) {
+  if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "rebased FP32 sweeps need a SINGLE or MIXED context");
+  gfx_status s;
+  if (!ctx->Ur && (s = dalloc(ctx, &ctx->Ur, link_bytes32(ctx)))) return s;
+  if (!ctx->W0 && (s = dalloc(ctx, &ctx->W0, rebased_w0_bytes(ctx->L)))) return s;
+  if ((s = ensure_scratch(ctx, link_bytes32(ctx)))) return s;
+  if ((s = sync_g64(ctx))) return s;
+  launch_rebase(ctx->link_nr, ndir, ctx->L, ctx->U64, ctx->G64, ctx->Ur, ctx->scratch_aos,
+                ctx->W0, ctx->stream);
+  CK(cudaMemsetAsync(ctx->G32, 0, g_bytes32(ctx), ctx->stream));
+  CK(cudaGetLastError());
+  ctx->g_active = 3;
+  ctx->rb_valid = true;
+  ctx->rb_ndir = ndir;
+  return GFX_OK;
+}
+
+gfx_status prepare_rebased(gfx_ctx* ctx, int ndir) {
+  if (ctx->g_active == 3 && ctx->rb_valid && ctx->rb_ndir == ndir) return GFX_OK;
+  return rebase(ctx, ndir);
 }
 
 // the double-float fields of the polish sweeps, allocated on first use; the links
@@ -127,7 +156,7 @@ gfx_status prepare_g(gfx_ctx* ctx, int prec) {
   if (prec == 2) {
     gfx_status s = ensure_df(ctx);
     if (s) return s;
-    if (ctx->g_active == 0 && (s = sync_g64(ctx))) return s;
+    if ((ctx->g_active == 0 || ctx->g_active == 3) && (s = sync_g64(ctx))) return s;
     if (ctx->g_active == 1) {
       launch_convert_g_df(1, ctx->L, ctx->G64, ctx->Gdf, ctx->stream);
       CK(cudaGetLastError());
@@ -137,7 +166,7 @@ gfx_status prepare_g(gfx_ctx* ctx, int prec) {
   }
   if (prec == 0) {
     if (!ctx->G32) return fail(ctx, GFX_ERR_STATE, "FP32 sweeps need a SINGLE or MIXED context");
-    if (ctx->g_active == 2) {
+    if (ctx->g_active >= 2) {
       gfx_status s = sync_g64(ctx);
       if (s) return s;
     }
@@ -154,6 +183,12 @@ gfx_status prepare_g(gfx_ctx* ctx, int prec) {
 }
 
 void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
+  if (prec == 3) {  // rebased FP32 (after prepare_rebased)
+    for (int p = 0; p < 2; p++)
+      launch_or_rebased(ndir, ctx->L, ctx->Ur, ctx->W0, ctx->G32, p, omega, ctx->stream);
+    ctx->launches += 2;
+    return;
+  }
   const void* U = prec == 0 ? ctx->U32 : prec == 2 ? ctx->Udf : ctx->U64;
   void* G = prec == 0 ? ctx->G32 : prec == 2 ? ctx->Gdf : ctx->G64;
   for (int p = 0; p < 2; p++)
@@ -175,6 +210,11 @@ static int meas_block(const gfx_ctx* ctx) {
 
 void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
   const int b = meas_block(ctx);
+  if (cprec == 3) {  // rebased FP32 (after prepare_rebased)
+    launch_measure_rebased(ndir, ctx->L, ctx->Ur, ctx->W0, ctx->G32, ctx->partials, b, ctx->stream);
+    ctx->launches += 1;
+    return;
+  }
   const void* U = cprec == 0 ? ctx->U32 : cprec == 2 ? ctx->Udf : ctx->U64;
   const void* G = gprec == 0 ? ctx->G32 : gprec == 2 ? ctx->Gdf : ctx->G64;
   launch_measure(cprec, lnr(ctx, cprec), gprec, ndir, ctx->L, U, G, ctx->partials, b, ctx->stream);
@@ -266,7 +306,7 @@ gfx_status gfx_destroy(gfx_ctx* ctx) {
   void* ptrs[] = {ctx->U64,     ctx->G64,  ctx->U32,  ctx->G32,  ctx->partials,
                   ctx->slice_sums, ctx->reduced, ctx->loop, ctx->hist, ctx->scratch_aos,
                   ctx->bank.a,  ctx->bank.b, ctx->bank.c, ctx->bank.seed, ctx->bank.status,
-                  ctx->gauss,   ctx->unif, ctx->Udf, ctx->Gdf};
+                  ctx->gauss,   ctx->unif, ctx->Udf, ctx->Gdf, ctx->Ur, ctx->W0};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (ctx->loop_host) cudaFreeHost(ctx->loop_host);
@@ -307,6 +347,9 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 0;
   ctx->Udf = ctx->Gdf = nullptr;
   ctx->udf_valid = false;
+  ctx->Ur = ctx->W0 = nullptr;
+  ctx->rb_valid = false;
+  ctx->rb_ndir = 0;
   ctx->tune_sweep_ms[0] = ctx->tune_sweep_ms[1] = 0.0;
   ctx->tune_measure_ms[0] = ctx->tune_measure_ms[1] = 0.0;
   ctx->tune_ck = 0;
@@ -499,10 +542,17 @@ gfx_status gfx_unit_trafo(gfx_ctx* ctx) {
 gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, int precision) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
   if (parity < 0 || parity > 1) return fail(ctx, GFX_ERR_ARG, "parity must be 0 or 1");
-  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
-  gfx_status s = prepare_g(ctx, prec);
-  if (s) return s;
+  // 2: double-float, 3: rebased FP32
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : precision == 3 ? 3 : 1;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  gfx_status s = prec == 3 ? prepare_rebased(ctx, ndir) : prepare_g(ctx, prec);
+  if (s) return s;
+  if (prec == 3) {
+    launch_or_rebased(ndir, ctx->L, ctx->Ur, ctx->W0, ctx->G32, parity, omega, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GFX_OK;
+  }
   launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
                       prec == 0 ? ctx->G32 : ctx->G64, parity, omega, ctx->or_block[prec],
                       ctx->or_pf[prec], ctx->stream);
@@ -513,10 +563,11 @@ gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, i
 
 gfx_status gfx_or_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision) {
   if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
-  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
-  gfx_status s = prepare_g(ctx, prec);
-  if (s) return s;
+  // 2: double-float, 3: rebased FP32
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : precision == 3 ? 3 : 1;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  gfx_status s = prec == 3 ? prepare_rebased(ctx, ndir) : prepare_g(ctx, prec);
+  if (s) return s;
   enqueue_sweeps(ctx, prec, ndir, omega, nsweeps);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
@@ -526,13 +577,16 @@ gfx_status gfx_or_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int
 gfx_status gfx_functional(gfx_ctx* ctx, int gauge, int precision, gfx_functional_t* out) {
   if (!ctx || !out) return fail(ctx, GFX_ERR_ARG, "gfx_functional: NULL argument");
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
-  int cprec = precision == 0 ? 0 : 1;
+  int cprec = precision == 0 ? 0 : precision == 3 ? 3 : 1;
   if (cprec == 0 && !ctx->U32) cprec = 1;
-  if (cprec == 0 || ctx->g_active == 2) {
+  if (cprec == 3) {
+    gfx_status s = prepare_rebased(ctx, ndir);
+    if (s) return s;
+  } else if (cprec == 0 || ctx->g_active >= 2) {
     gfx_status s = prepare_g(ctx, cprec);
     if (s) return s;
   }
-  const int gprec = cprec == 0 ? 0 : ctx->g_active;
+  const int gprec = cprec == 0 ? 0 : cprec == 3 ? 3 : ctx->g_active;
   enqueue_measure(ctx, cprec, gprec, ndir);
   enqueue_reduce(ctx, ndir, false, 0, 0, 0);
   CK(cudaGetLastError());
@@ -651,6 +705,10 @@ static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double ome
   return GFX_OK;
 }
 
+// sweeps between two bases of the rebased FP32 polish: |a| grows slowly near
+// convergence, and a new base (about one FP64 sweep of work) keeps it small
+constexpr int kRebaseSweeps = 1000;
+
 static gfx_status read_loop(gfx_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->loop_host, ctx->loop, sizeof(LoopState), cudaMemcpyDeviceToHost,
                      ctx->stream));
@@ -675,6 +733,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   gfx_status s = prepare_g(ctx, prec);
   if (s) return s;
   if (p.checkinterval_near < 0) return fail(ctx, GFX_ERR_ARG, "checkinterval_near must be >= 0");
+  if (p.polish < 0 || p.polish > 2) return fail(ctx, GFX_ERR_ARG, "polish must be 0, 1 or 2");
   const int ck_min = std::min(std::min(p.checkinterval, p.checkinterval_double),
                               p.checkinterval_near > 0 ? p.checkinterval_near : p.checkinterval);
   const int hist_need = p.maxit / ck_min + 8;
@@ -707,7 +766,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   s = write_loop(ctx);
   if (s) return s;
 
-  int sweeps_single = 0, sweeps_double = 0, sweeps_df = 0;
+  int sweeps_single = 0, sweeps_double = 0, sweeps_df = 0, sweeps_rb = 0;
   // iteration 0: sweep, then the first check (overrelax.cu:710-789)
   enqueue_sweeps(ctx, prec, ndir, p.omega, 1);
   (prec == 0 ? sweeps_single : sweeps_double)++;
@@ -740,6 +799,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       }
       (prec == 0 ? sweeps_single : sweeps_double) += H.iter - it0;
       if (prec == 2) sweeps_df += H.iter - it0;
+      if (prec == 3) sweeps_rb += H.iter - it0;
     }
     if (H.done == 4) {
       // below switch_eps: the same phase continues with the shorter interval
@@ -749,13 +809,23 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       if (s) return s;
       continue;
     }
-    if (H.done == 1 && prec == 2) {
-      // the double-float polish reached eps: confirm with an FP64 measurement; if it
-      // does not, FP64 sweeps continue
+    if (H.done == 5) {
+      // rebased FP32 polish: a new base from the current g
+      if (prec == 3 && (s = rebase(ctx, ndir))) return s;
+      H.rebase_at = prec == 3 ? H.iter + kRebaseSweeps : 0;
+      H.done = 0;
+      s = write_loop(ctx);
+      if (s) return s;
+      continue;
+    }
+    if (H.done == 1 && prec >= 2) {
+      // the double-float or rebased FP32 polish reached eps: confirm with an FP64
+      // measurement; if it does not, FP64 sweeps continue
       s = prepare_g(ctx, 1);
       if (s) return s;
       prec = 1;
       H.done = 0;
+      H.rebase_at = 0;
       s = write_loop(ctx);
       if (s) return s;
       enqueue_measure(ctx, 1, 1, ndir);
@@ -770,8 +840,10 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       // double-float; the first check verifies the handover state
       s = prepare_g(ctx, 1);
       if (s) return s;
-      prec = p.polish ? 2 : 1;
+      prec = p.polish == 2 ? 3 : p.polish == 1 ? 2 : 1;
       if (prec == 2 && (s = prepare_g(ctx, 2))) return s;
+      if (prec == 3 && (s = rebase(ctx, ndir))) return s;
+      H.rebase_at = prec == 3 ? H.iter + kRebaseSweeps : 0;
       H.phase = 1;
       H.done = 0;
       H.prev = 0.0;
@@ -795,6 +867,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
     enqueue_sweeps(ctx, prec, ndir, p.omega, tail);
     (prec == 0 ? sweeps_single : sweeps_double) += tail > 0 ? tail : 0;
     if (prec == 2) sweeps_df += tail > 0 ? tail : 0;
+    if (prec == 3) sweeps_rb += tail > 0 ? tail : 0;
     if (prec == 0 && handover) {
       s = prepare_g(ctx, 1);
       if (s) return s;
@@ -827,6 +900,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
     res->sweeps_double = sweeps_double;
     res->sweeps = sweeps_single + sweeps_double;
     res->sweeps_polish_df = sweeps_df;
+    res->sweeps_polish_fp32 = sweeps_rb;
     res->checks = H.nhist;
     res->final_values.F = H.last_F;
     res->final_values.dAdA = H.last_dAdA;
@@ -1153,10 +1227,11 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
 gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, int precision,
                            double* ms) {
   if (!ctx || !ms || nsweeps < 1) return fail(ctx, GFX_ERR_ARG, "gfx_time_sweeps: bad argument");
-  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : 1;  // 2: double-float
-  gfx_status s = prepare_g(ctx, prec);
-  if (s) return s;
+  // 2: double-float, 3: rebased FP32
+  const int prec = precision == 0 ? 0 : precision == 2 ? 2 : precision == 3 ? 3 : 1;
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
+  gfx_status s = prec == 3 ? prepare_rebased(ctx, ndir) : prepare_g(ctx, prec);
+  if (s) return s;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));

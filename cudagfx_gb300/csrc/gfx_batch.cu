@@ -67,7 +67,7 @@ __device__ __forceinline__ int conf_of(const BDesc& d, int item, int BConf::*bas
 // site) come from L2 for all but the first copy; each link crosses HBM about once per
 // half-sweep whatever the number of copies.
 template <typename T, int NDIR>
-__global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 1) or_batch_kernel(BDesc d, int parity, T omega) {
+__global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_kernel(BDesc d, int parity, T omega) {
   typedef typename VecOf<T>::type V;
   constexpr int NC = Field<T, 12>::NCHUNK;
   const int ci = conf_of(d, blockIdx.x, &BConf::item_base);

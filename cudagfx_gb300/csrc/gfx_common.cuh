@@ -301,7 +301,7 @@ enum { CRIT_MAXDADA = 0, CRIT_THETA = 1, CRIT_THETA_SLICES = 2 };
 
 // Totals over the slices, then (when loop is given) one check of the convergence loop:
 // record, compare with the criterion, decide done (0 run on, 1 converged, 2 leave the
-// FP32 phase, 3 iteration cap).  Called by all threads of one block; returns done on
+// FP32 phase, 3 iteration cap, 4 shorter check interval, 5 renew the rebased base).  Called by all threads of one block; returns done on
 // thread 0 (and -1 elsewhere).
 __device__ __forceinline__ int reduce_and_check(const double* slice_sums, int lt, double vol,
                                                 double v3, int ndir, Reduced* out,
@@ -382,6 +382,7 @@ __device__ __forceinline__ int reduce_and_check(const double* slice_sums, int lt
   // the FP32 floor) while the long interval keeps the checks cheap before that
   if (!done && S.ck_near > 0 && S.ck > S.ck_near && value < S.switch_eps) done = 4;
   if (!done && S.iter + S.ck >= S.maxit) done = 3;
+  if (!done && S.rebase_at > 0 && S.iter >= S.rebase_at) done = 5;
   S.prev = value;
   S.done = done;
   return done;

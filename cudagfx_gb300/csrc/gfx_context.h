@@ -14,6 +14,7 @@
 //   G64 : gauge transformation, FP64, 12 reals
 //   U32, G32 : FP32 copies for the single/mixed-precision sweeps (links 12 or 8 reals)
 //   Udf, Gdf : double-float copies for the polish sweeps
+//   Ur, W0 : the base of the rebased FP32 polish sweeps (gfx_rebased.cu)
 // and the work buffers of the reductions, the convergence loop and the twister bank.
 struct gfx_ctx {
   int lx, ly, lz, lt;
@@ -30,10 +31,15 @@ struct gfx_ctx {
   int tune_ck;
   cudaStream_t stream;
   bool own_stream;
-  int g_active;  // 0: G32 holds the current g, 1: G64 does, 2: Gdf does
+  int g_active;  // 0: G32 holds the current g, 1: G64 does, 2: Gdf does,
+                 // 3: g = (1 + a) G64 with a in G32 (rebased FP32 sweeps)
   void* Udf;     // double-float links (18 reals) and g (12 reals) of the polish sweeps
   void* Gdf;
   bool udf_valid;
+  void* Ur;      // rebased FP32 sweeps: links g_c U g_c^+ (FP32, 12 reals) and split star
+  void* W0;
+  bool rb_valid;  // Ur and W0 belong to the current base, links and rb_ndir
+  int rb_ndir;
   // fields
   void* U64;
   void* G64;
@@ -118,6 +124,10 @@ gfx_status sync_g64(gfx_ctx* ctx);
 gfx_status ensure_df(gfx_ctx* ctx);
 // make the g of precision prec (0 FP32, 1 FP64, 2 double-float) the current one
 gfx_status prepare_g(gfx_ctx* ctx, int prec);
+// a new base for the rebased FP32 sweeps over ndir directions: g_c = g, a = 0
+gfx_status rebase(gfx_ctx* ctx, int ndir);
+// the rebased state for ndir directions, keeping a valid base
+gfx_status prepare_rebased(gfx_ctx* ctx, int ndir);
 void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega);
 void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
 void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir);

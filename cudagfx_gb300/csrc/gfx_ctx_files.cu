@@ -107,7 +107,7 @@ gfx_status gfx_checkpoint_save(gfx_ctx* ctx, const char* path) {
   }
   std::vector<double> g(18 * (size_t)ctx->vol);
   if ((s = gfx_get_trafo(ctx, g.data()))) return s;
-  ctx->g_active = active;  // gfx_get_trafo widened a current FP32 g; it stays current
+  if (active == 0) ctx->g_active = 0;  // gfx_get_trafo widened a current FP32 g; it stays current
   char info[512];
   std::snprintf(info, sizeof(info),
                 "gfx-checkpoint 1\ndims %d %d %d %d\nprecision %d\nlink_reals %d\ng_fp32 %d\n"

@@ -25,11 +25,13 @@ struct LoopState {
   int ck;         // sweeps between checks
   int maxit;      // iteration cap (exclusive, as in the reference loop)
   int done;       // 0 running, 1 converged, 2 switch precision, 3 stopped at cap,
-                  // 4 below switch_eps: continue with ck_near sweeps between checks
+                  // 4 below switch_eps: continue with ck_near sweeps between checks,
+                  // 5 renew the base of the rebased FP32 sweeps
   int ck_near;    // sweeps between checks once the value is below switch_eps (0: ck)
   int criterion;  // GFX_CRIT_*
   int phase;
   int nhist, hist_cap;
+  int rebase_at;  // > 0: done = 5 at the first check with iter >= rebase_at
   double eps;
   double switch_eps;     // phase 0 -> 1 when the monitored value drops below
   double plateau_ratio;  // phase 0 -> 1 when value_new > plateau_ratio * value_old (ck sweeps apart)
@@ -77,6 +79,18 @@ void launch_convert_links_64_to_32(int link_nr, int link_nr32, const Lattice& L,
 void launch_convert_g(int from_prec, int to_prec, const Lattice& L, const void* Gin, void* Gout,
                       cudaStream_t s);
 void launch_apply_trafo(int link_nr, const Lattice& L, void* U64, const void* G64, cudaStream_t s);
+// ----- rebased FP32 sweeps (gfx_rebased.cu): g = (1 + a) g_c, a in FP32 (G32 layout) -----
+// base: Ur = rebased links (FP32 12-real layout), Ulo = their FP32 remainders (same
+// size, scratch), W0 = the split star (rebased_w0_bytes); ndir directions
+size_t rebased_w0_bytes(const Lattice& L);
+void launch_rebase(int link_nr, int ndir, const Lattice& L, const void* U64, const void* G64,
+                   void* Ur, void* Ulo, void* W0, cudaStream_t s);
+// G64 <- normalize((1 + a) G64) in FP64
+void launch_compose_g(const Lattice& L, void* G64, const void* A, cudaStream_t s);
+void launch_or_rebased(int ndir, const Lattice& L, const void* Ur, const void* W0, void* A,
+                       int parity, double omega, cudaStream_t s);
+void launch_measure_rebased(int ndir, const Lattice& L, const void* Ur, const void* W0,
+                            const void* A, double* partials, int block, cudaStream_t s);
 // Haar-random FP64 g: the value at lexicographic site pos depends only on (seed, pos)
 void launch_haar_g(const Lattice& L, double2* G64, unsigned long long seed, cudaStream_t s);
 

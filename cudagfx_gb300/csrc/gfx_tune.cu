@@ -166,7 +166,9 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
     ctx->tune_ck = suggest_checkinterval(ctx, expected_sweeps);
     return out ? gfx_get_tuning(ctx, out) : GFX_OK;
   }
-  // keep the current g: the candidate sweeps run on it
+  // keep the current g: the candidate sweeps run on it (from G64 when it is held as
+  // double-float or on a rebased base)
+  if (ctx->g_active >= 2 && (s = sync_g64(ctx))) return s;
   const int active = ctx->g_active;
   void* gsrc = active ? ctx->G64 : ctx->G32;
   const size_t gbytes = active ? g_bytes64(ctx) : g_bytes32(ctx);

@@ -76,9 +76,12 @@ typedef struct {
   int checkinterval_near; /* sweeps between checks once the value is below switch_eps
                              (0: checkinterval throughout, the reference schedule) */
   int polish;             /* mixed: 0 = FP64 sweeps after the handover; 1 = double-float
-                             sweeps (pairs of floats, ~48 bits) on the FP32 units, whose
-                             result an FP64 measurement confirms (FP64 sweeps continue if
-                             it does not).  GB300 runs FP32 64x faster than FP64. */
+                             sweeps (pairs of floats, ~48 bits) on the FP32 units; 2 =
+                             rebased FP32 sweeps: g = (1 + a) g_c with g_c fixed in FP64
+                             and only the small a in FP32, which follow the FP64 sweeps
+                             to ~1e-12 at FP32 cost.  The result of 1 and 2 is confirmed
+                             by an FP64 measurement (FP64 sweeps continue if it is not).
+                             GB300 runs FP32 64x faster than FP64. */
 } gfx_or_params;
 
 typedef struct {
@@ -91,6 +94,7 @@ typedef struct {
   gfx_functional_t final_values; /* last evaluation (FP64 unless precision is SINGLE) */
   double ms;          /* device time of the whole call (CUDA events) */
   int sweeps_polish_df; /* of sweeps_double, those run in double-float (polish = 1) */
+  int sweeps_polish_fp32; /* of sweeps_double, those run as rebased FP32 (polish = 2) */
 } gfx_or_result;
 
 typedef struct {
@@ -201,11 +205,14 @@ gfx_status gfx_overrelax(gfx_ctx *ctx, const gfx_or_params *p, gfx_or_result *re
 /* copy up to cap check records of the last gfx_overrelax call; returns the count */
 int gfx_or_history(const gfx_ctx *ctx, gfx_check_record *out, int cap);
 /* nsweeps plain OR sweeps (even then odd) without checks; precision 0 = FP32, 1 = FP64,
- * 2 = double-float (the polish sweeps of gfx_or_params.polish = 1) */
+ * 2 = double-float (the polish sweeps of gfx_or_params.polish = 1), 3 = rebased FP32 (the
+ * polish sweeps of polish = 2; a base is taken from the current g unless the last call
+ * left one for the same gauge and links) */
 gfx_status gfx_or_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision);
 /* one OR half-sweep of one parity */
 gfx_status gfx_or_halfsweep(gfx_ctx *ctx, int parity, double omega, int gauge, int precision);
-/* calc_functional (overrelax.cu:610-671); precision 0 = FP32 arithmetic, 1 = FP64 */
+/* calc_functional (overrelax.cu:610-671); precision 0 = FP32 arithmetic, 1 = FP64,
+ * 3 = rebased FP32 (the checks of polish = 2) */
 gfx_status gfx_functional(gfx_ctx *ctx, int gauge, int precision, gfx_functional_t *out);
 /* calc_plaquette (overrelax.cu:115-138) on the links */
 gfx_status gfx_plaquette(gfx_ctx *ctx, double *plaq);

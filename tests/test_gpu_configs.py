@@ -5,9 +5,9 @@ checks: convergence verified in FP64, mixed vs all-FP64 agreement, gauge invaria
       (linear), 3 microcanonical steps per heatbath step, then OR omega 1.7 to
       theta < 1e-12, mixed against all-FP64 from the same annealed g.
   C3  32^4, beta 6.0 (seed 42), Coulomb gauge: every time slice to theta_t < 1e-15,
-      mixed (double-float polish) against all-FP64; plaquette and Polyakov loop
+      mixed (rebased FP32 polish) against all-FP64; plaquette and Polyakov loop
       unchanged to 1e-12.
-  C5  48^3x96, beta 6.2, FP64 18-real links: SA then mixed OR (double-float polish,
+  C5  48^3x96, beta 6.2, FP64 18-real links: SA then mixed OR (rebased FP32 polish,
       FP64-confirmed) to theta < 1e-14.  The
       thermalization (20 instead of 1000 heatbath sweeps) and the annealing (50 instead
       of 1000 steps) are shortened to keep the test under a minute; the lattice size,
@@ -72,7 +72,7 @@ def test_c3_coulomb_slices(mt_params):
     src.close()
     g0 = gfx.random_init_reference(351, V)
     kw = dict(maxit=20000, eps=1e-15, checkinterval=50, omega=1.7, gauge=gfx.COULOMB,
-              criterion=gfx.CRIT_THETA_SLICES, polish=1)
+              criterion=gfx.CRIT_THETA_SLICES, polish=2)
     out = {}
     for prec in (gfx.PREC_MIXED, gfx.PREC_DOUBLE):
         c = gfx.Context(dims, precision=prec)
@@ -99,7 +99,7 @@ def test_c5_large_lattice_fp64_links(mt_params):
     c.set_trafo(gfx.random_init_reference(351, V))
     c.simanneal(0.01, 1.0, 50, expo=-1.0, checkint=50, nmicro=3)
     r = c.overrelax(maxit=20000, eps=1e-14, checkinterval=100, omega=1.7,
-                    criterion=gfx.CRIT_THETA, checkinterval_near=10, polish=1)
+                    criterion=gfx.CRIT_THETA, checkinterval_near=10, polish=2)
     assert r.converged and r.final_values.theta < 1e-14
     assert r.sweeps_double > 0  # below the FP32 floor only FP64 sweeps get there
     f = c.functional(precision=1)
