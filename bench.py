@@ -41,8 +41,9 @@ BYTES_PER_UPDATE_FP32 = 132 * 4
 BYTES_PER_UPDATE_FP64 = 132 * 8
 FLOP_PER_UPDATE = 4766  # the reference's count (overrelax.cu:897)
 # DRAM bytes per FP32 half-sweep launch at 32^4 (dram__bytes_read.sum +
-# dram__bytes_write.sum), from the ncu capture in profiles/or_halfsweep_fp32_32x4.md
-NCU_TRAFFIC_FP32 = {(32, 32, 32, 32): 254.05e6 + 15.68e6}
+# dram__bytes_write.sum) in the alternating sweep with warm L2 (staging 2), from the
+# --cache-control none capture in profiles/or_halfsweep_fp32_32x4.md
+NCU_TRAFFIC_FP32 = {(32, 32, 32, 32): 198.4e6 + 27.2e6}
 
 
 POLISH_NAMES = {0: "FP64", 1: "double-float (FP32 pairs), FP64-confirmed",
@@ -78,6 +79,8 @@ def parse():
                     help="skip the batched-Gribov-copies measurement")
     ap.add_argument("--gribov-copies", default="64,32",
                     help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
+    ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2],
+                    help="--kernels: OR half-sweep staging mode")
     ap.add_argument("--kernels", action="store_true",
                     help="no timing: a few launches of each hot kernel on the lattice, for "
                          "ncu captures")
@@ -141,16 +144,22 @@ def gribov_batch(args, gfx, mt_source):
 
 def run_kernels(args, dims):
     """A short fixed workload for profiler captures: 3 FP32 OR sweeps, an FP32 and an
-    FP64 functional, 1 FP64 OR sweep, one SA step and one link-heatbath sweep."""
+    FP64 functional, 1 FP64 OR sweep, 3 rebased FP32 sweeps and their functional, one
+    SA step and one link-heatbath sweep.  The OR sweeps use --staging (2, the tuner's
+    choice on 32^4: the odd half-sweep in reverse block order)."""
     import cudagfx_gb300 as gfx
     V = int(np.prod(dims))
     ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    t = ctx.tuning()
+    ctx.set_tuning(block=t["block"], staging=(args.staging, args.staging))
     ctx.set_links(gfx.random_init_haar(11, 4 * V))
     ctx.set_trafo(gfx.random_init_reference(351, V))
     ctx.or_sweeps(3, omega=args.omega, precision=0)
     ctx.functional(precision=0)
     ctx.functional(precision=1)
     ctx.or_sweeps(1, omega=args.omega, precision=1)
+    ctx.or_sweeps(3, omega=args.omega, precision=3)
+    ctx.functional(precision=3)
     dat = mt_params_path()
     if dat:
         ctx.mt_load_file(dat)

@@ -296,7 +296,8 @@ class Context:
 
     def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0,
                    link_reals32=0):
-        """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first."""
+        """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first,
+        2 plain loads with the odd half-sweep's blocks in reverse order."""
         t = Tuning()
         t.block[0], t.block[1] = block
         t.staging[0], t.staging[1] = staging

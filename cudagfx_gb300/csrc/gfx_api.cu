@@ -344,7 +344,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->link_nr32 = 12;
   ctx->block = 128;
   ctx->or_block[0] = ctx->or_block[1] = ctx->or_block[2] = 128;
-  ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 0;
+  ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 2;  // odd half-sweeps in reverse order
   ctx->Udf = ctx->Gdf = nullptr;
   ctx->udf_valid = false;
   ctx->Ur = ctx->W0 = nullptr;

@@ -70,9 +70,12 @@ template <typename T, int NDIR>
 __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_kernel(BDesc d, int parity, T omega) {
   typedef typename VecOf<T>::type V;
   constexpr int NC = Field<T, 12>::NCHUNK;
-  const int ci = conf_of(d, blockIdx.x, &BConf::item_base);
+  // parity 1 runs the work items in reverse order: it starts on the ranges parity 0
+  // touched last, which L2 may still hold (the order does not change any result)
+  const int item = parity ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+  const int ci = conf_of(d, item, &BConf::item_base);
   const BConf& C = d.c[ci];
-  const int local = blockIdx.x - C.item_base;
+  const int local = item - C.item_base;
   const int blk = local / C.ncopies, copy = local - blk * C.ncopies;
   if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
   const int i = blk * kBatchBlock + threadIdx.x;

@@ -26,7 +26,8 @@ struct gfx_ctx {
   size_t u32_bytes;
   int block;
   int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
-  int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch
+  int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch, 2 plain
+                    // with the odd half-sweep's blocks in reverse order (the default)
   double tune_sweep_ms[2], tune_measure_ms[2];
   int tune_ck;
   cudaStream_t stream;

@@ -49,7 +49,8 @@ struct Reduced {
 // prec: 0 FP32, 1 FP64, 2 double-float (links 18 reals, g 12 reals, float pairs).
 // link_nr arguments give the layout of the link field read: FP32 12 or 8 reals when
 // prec == 0, FP64 12 or 18 reals when prec == 1
-// mode: 0 plain loads, 1 L2 bulk prefetch per block
+// mode: 0 plain loads, 1 L2 bulk prefetch per block, 2 plain loads with the blocks of
+// parity 1 in reverse order
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
                          int parity, double omega, int block, int mode, cudaStream_t s);
 // measure: compute precision (0 float, 1 double), g storage (0 float, 1 double)

@@ -39,20 +39,24 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // ---------------------------------------------------------------------------
 // overrelaxation half-sweep (overrelax.cu:335-446), in place on parity `parity`
 // ---------------------------------------------------------------------------
-// MODE (launch_or_halfsweep's mode): 0 plain loads; 1 each block first issues one
-// L2 bulk prefetch per contiguous range it reads.
+// MODE (launch_or_halfsweep's mode 0/1): 0 plain loads; 1 each block first issues one
+// L2 bulk prefetch per contiguous range it reads.  rev != 0 runs the blocks in reverse
+// index order: after a half-sweep in forward order, the next one then starts on the
+// ranges the previous one touched last, which L2 may still hold.  The sites of one
+// parity are independent, so the order does not change the result.
 template <typename T, int NRU, int NDIR, int MODE>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) or_halfsweep_kernel(Lattice L,
                                                             const typename VecOf<T>::type* U,
                                                             typename VecOf<T>::type* G, int parity,
-                                                            T omega) {
+                                                            T omega, int rev) {
   constexpr int NCG = Field<T, 12>::NCHUNK;
   constexpr int NCU = Field<T, NRU>::NCHUNK;
+  const int blk = rev ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
   if (MODE == 1) {
-    const int i0 = blockIdx.x * blockDim.x;
+    const int i0 = blk * blockDim.x;
     prefetch_block<NCU, NCG, NDIR>(L, parity, i0, min((int)blockDim.x, L.vh - i0), U, G);
   }
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blk * blockDim.x + threadIdx.x;
   if (i >= L.vh) return;
   const Site c = site_of(L, i, parity);
   or_site_update<T, NRU, NDIR>(L, c, parity, U, G, i, omega);
@@ -66,9 +70,10 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
     const auto* u_ = (const typename VecOf<T>::type*)U;                                          \
     auto* g_ = (typename VecOf<T>::type*)G;                                                      \
     if (mode == 1)                                                                               \
-      or_halfsweep_kernel<T, NR, ND, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
+      or_halfsweep_kernel<T, NR, ND, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega, 0);  \
     else                                                                                         \
-      or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega);     \
+      or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega,      \
+                                                               mode == 2 ? parity : 0);          \
   } while (0)
   if (prec == 2) {  // double-float, 18-real links
     if (ndir == 4) OR_LAUNCH(dfl, 18, 4);

@@ -33,7 +33,7 @@ namespace gfx {
 //   21..26 AH(lo)_01, AH(lo)_02, AH(lo)_12                  (re, im); AH(lo)_ba = -conj(AH(lo)_ab)
 //   27     Re tr lo
 constexpr int kW0Planes = 7;
-constexpr int kRebasedBlock = 256;
+constexpr int kRebasedBlock = 128;
 
 // ---------------------------------------------------------------------------
 // base construction (FP64)
@@ -416,12 +416,14 @@ __device__ __forceinline__ void or_update_small(const Mat3<float>& Xh, const Mat
 }
 
 template <int NDIR>
-__global__ void __launch_bounds__(kRebasedBlock, 2) or_rebased_kernel(Lattice L,
+__global__ void __launch_bounds__(kRebasedBlock, 4) or_rebased_kernel(Lattice L,
                                                                       const float4* __restrict__ Ur,
                                                                       const float4* __restrict__ W0,
                                                                       float4* __restrict__ A,
                                                                       int parity, float omega) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // parity 1 in reverse block order: it starts where parity 0 ended (L2 reuse)
+  const int blk = parity ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+  const int i = blk * blockDim.x + threadIdx.x;
   if (i >= L.vh) return;
   const Site c = site_of(L, i, parity);
   Mat3<float> Xh, Xd, a, b;

@@ -152,8 +152,10 @@ gfx_status gfx_set_block(gfx_ctx *ctx, int block);
  * Settings of the overrelaxation half-sweep per precision, [0] = FP32 storage,
  * [1] = FP64.  block: threads per block (a multiple of 32 in [32, 256]).
  * staging: 0 = plain 128-bit loads; 1 = each block first issues one L2 bulk
- * prefetch (cp.async.bulk.prefetch.L2) per contiguous range it reads.  All
- * settings give bit-identical results.
+ * prefetch (cp.async.bulk.prefetch.L2) per contiguous range it reads; 2 = plain
+ * loads, and the odd half-sweep runs its blocks in reverse order, so that it starts
+ * on the ranges the even half-sweep touched last (still in L2).  All settings give
+ * bit-identical results.
  * link_reals64: FP64 link storage, 12 (two rows) or 18 (full).  link_reals32: the
  * FP32 copy the FP32 sweeps read, 12 or 8.  The 8-real form rebuilds rows 1, 2
  * dividing by |U_01|^2 + |U_02|^2; the few links where that is below 1e-2 are read
@@ -179,7 +181,7 @@ gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
  * change of link_reals64 re-packs the FP64 links on the device. */
 gfx_status gfx_set_tuning(gfx_ctx *ctx, const gfx_tuning *t);
 /* Time every candidate setting on this context's lattice and apply the fastest.
- * Candidates: block 64/128/192/256 x staging 0/1 for each precision the
+ * Candidates: block 64/128/192/256 x staging 0/1/2 for each precision the
  * context holds, and both link layouts of each precision.  The fields are left as they
  * were: the candidate sweeps run on g and it is restored afterwards.
  * expected_sweeps > 0 also sets checkinterval to the interval that minimises

@@ -1,4 +1,5 @@
-"""Launch tuning: every block size, both staging modes (plain loads, L2 bulk prefetch)
+"""Launch tuning: every block size, every staging mode (plain loads, L2 bulk prefetch,
+odd half-sweep in reverse block order)
 and both FP64 link layouts give bit-identical sweeps; gfx_autotune leaves the fields as it found them, its
 choice reproduces the untuned solve exactly, and its cache file round-trips."""
 import numpy as np
@@ -28,7 +29,7 @@ def test_launch_variants_are_bit_identical(prec):
     ref.close()
     for nr in ((12, 18) if prec == 1 else (12,)):
         for block in (32, 64, 96, 128, 192, 256):
-            for pf in (0, 1):
+            for pf in (0, 1, 2):
                 c = _ctx()
                 c.set_tuning(block=(block, block), staging=(pf, pf), link_reals64=nr)
                 c.or_sweeps(3, omega=1.7, precision=prec)
@@ -45,7 +46,7 @@ def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
     ga = a.get_trafo()
     b = _ctx()
     t = b.autotune(expected_sweeps=1000, cache_path=str(tmp_path / "tune.txt"))
-    assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1)
+    assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1, 2)
     assert t["link_reals64"] in (12, 18) and 5 <= t["checkinterval"] <= 100
     assert t["link_reals32"] in (12, 8)
     assert t["sweep_ms"][0] > 0 and t["check_ms"][1] > 0
@@ -81,7 +82,7 @@ def test_autotune_cache_hit_applies_stored_settings(tmp_path):
 
 def test_set_tuning_rejects_bad_settings():
     c = _ctx()
-    for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(2, 0)), dict(staging=(0, -1)),
+    for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(3, 0)), dict(staging=(0, -1)),
                 dict(link_reals64=8), dict(link_reals32=18)):
         with pytest.raises(gfx.GfxError):
             c.set_tuning(**bad)
