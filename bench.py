@@ -89,15 +89,17 @@ def parse():
 
 def gribov_batch(args, gfx, mt_source):
     """Batched Gribov copies: 64 copies of a 16^4 beta=6.0 configuration and 32 copies of
-    a 24^4 beta=6.2 configuration, Haar-random starts (seed 2024 + copy), mixed FP32->FP64
-    OR omega=1.7 to theta<1e-12, the largest-functional copy kept per configuration.
+    a 24^4 beta=6.2 configuration, Haar-random starts (seed 2024 + copy), mixed OR
+    omega=1.7 (FP32, then the --polish sweeps; double-float is not batched and falls
+    back to FP64) to theta<1e-12, the largest-functional copy kept per configuration.
     Batched: one device loop for all copies.  Sequential: the same starts, one
     single-lattice solve per copy.  Both timed with CUDA events (solve only)."""
     confs = [((16, 16, 16, 16), 6.0), ((24, 24, 24, 24), 6.2)]
     ncopies = [int(x) for x in args.gribov_copies.split(",")]
     kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval or 25, omega=args.omega,
               criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
-              checkinterval_double=args.checkinterval_double)
+              checkinterval_double=args.checkinterval_double,
+              polish=2 if args.polish == 2 else 0)
     links = []
     for k, (d, beta) in enumerate(confs):
         V = int(np.prod(d))
@@ -134,6 +136,7 @@ def gribov_batch(args, gfx, mt_source):
         c.close()
     return {"workload": "%d x 16^4 (beta 6.0) + %d x 24^4 (beta 6.2) Gribov copies, Haar starts, "
                         "theta<%g" % (ncopies[0], ncopies[1], args.eps),
+            "polish": POLISH_NAMES[kw["polish"]],
             "converged": sum(r["converged"] for r in res), "copies": len(res),
             "batched_s": ms_b / 1000.0, "sequential_s": ms_s / 1000.0,
             "batched_site_updates_per_s": upd / (ms_b / 1000.0),

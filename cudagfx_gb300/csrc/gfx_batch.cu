@@ -21,6 +21,7 @@
 #include "../../include/gfx.h"
 #include "gfx_common.cuh"
 #include "gfx_internal.h"
+#include "gfx_rebased.cuh"
 
 namespace gfx {
 
@@ -34,6 +35,9 @@ struct BConf {
   void* G32;         // copy 0's g (FP32), copy k at + k * gstride32 vectors
   void* G64;         // copy 0's g (FP64), copy k at + k * gstride64 vectors
   size_t gstride32, gstride64;
+  void* Ur;          // rebased FP32 polish (polish = 2): copy k's rebased links at
+  void* W0;          // + k * urstride vectors, its split star at + k * w0stride
+  size_t urstride, w0stride;
   int ncopies;
   int copy_base;     // index of copy 0 among all copies of the batch
   int item_base;     // first sweep work item
@@ -87,6 +91,25 @@ __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_
   or_site_update<T, 12, NDIR>(C.L, s, parity, U, G, i, omega);
 }
 
+// The rebased FP32 polish sweep for all active copies (or_rebased_kernel per copy, the
+// same work-item order as or_batch_kernel); a copy's a lives in its G32 slot
+template <int NDIR>
+__global__ void __launch_bounds__(kBatchBlock, 4) or_batch_rebased_kernel(BDesc d, int parity,
+                                                                          float omega) {
+  const int item = parity ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+  const int ci = conf_of(d, item, &BConf::item_base);
+  const BConf& C = d.c[ci];
+  const int local = item - C.item_base;
+  const int blk = local / C.ncopies, copy = local - blk * C.ncopies;
+  if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  const int i = blk * kBatchBlock + threadIdx.x;
+  if (i >= C.L.vh) return;
+  rebased_site_update<NDIR>(C.L, site_of(C.L, i, parity), parity,
+                            (const float4*)C.Ur + (size_t)copy * C.urstride,
+                            (const float4*)C.W0 + (size_t)copy * C.w0stride,
+                            (float4*)C.G32 + (size_t)copy * C.gstride32, omega);
+}
+
 // Per-copy functional partials (measure_kernel per copy, same block grouping)
 template <typename TC, typename TSG, int NDIR>
 __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
@@ -116,6 +139,31 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * C.L.vh, (size_t)C.L.vh, i, g);
     site_functional(g, star, f, dd);
   }
+  double* out = d.partials +
+                3 * (C.part_base + (size_t)copy * per_copy + (size_t)(parity * C.L.lt + t) * C.nbx + bx);
+  block_reduce3(f, dd, dd, out);
+}
+
+// the same partials from the rebased fields (measure_rebased_kernel per copy)
+template <int NDIR>
+__global__ void __launch_bounds__(kBatchBlock) measure_batch_rebased_kernel(BDesc d) {
+  const int ci = conf_of(d, blockIdx.x, &BConf::mitem_base);
+  const BConf& C = d.c[ci];
+  int local = blockIdx.x - C.mitem_base;
+  const int per_copy = 2 * C.L.lt * C.nbx;
+  const int copy = local / per_copy;
+  local -= copy * per_copy;
+  const int parity = local / (C.L.lt * C.nbx);
+  local -= parity * C.L.lt * C.nbx;
+  const int t = local / C.nbx, bx = local - t * C.nbx;
+  if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  const int k = bx * blockDim.x + threadIdx.x;
+  double f = 0.0, dd = 0.0;
+  if (k < C.L.st)
+    rebased_site_functional<NDIR>(C.L, site_of(C.L, t * C.L.st + k, parity), parity,
+                                  (const float4*)C.Ur + (size_t)copy * C.urstride,
+                                  (const float4*)C.W0 + (size_t)copy * C.w0stride,
+                                  (const float4*)C.G32 + (size_t)copy * C.gstride32, f, dd);
   double* out = d.partials +
                 3 * (C.part_base + (size_t)copy * per_copy + (size_t)(parity * C.L.lt + t) * C.nbx + bx);
   block_reduce3(f, dd, dd, out);
@@ -225,6 +273,7 @@ struct gfx_batch {
     cudaGraphExec_t exec;
   };
   std::vector<G> graphs;
+  void* ulo;  // scratch of the rebase: FP32 remainders of the largest configuration's links
   std::string err;
 };
 
@@ -258,7 +307,12 @@ gfx_status balloc(gfx_batch* b, void** p, size_t bytes) {
 void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
   const size_t sm = 0;
   for (int p = 0; p < 2; p++) {
-    if (prec == 0) {
+    if (prec == 3) {  // rebased FP32
+      if (ndir == 4)
+        or_batch_rebased_kernel<4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+      else
+        or_batch_rebased_kernel<3><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+    } else if (prec == 0) {
       if (ndir == 4)
         or_batch_kernel<float, 4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
       else
@@ -274,7 +328,10 @@ void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
 
 void enqueue_check(gfx_batch* b, int cprec, int gprec, int ndir, int advance,
                    unsigned long long handle, int use_handle) {
-  if (cprec == 0) {
+  if (cprec == 3) {
+    if (ndir == 4) measure_batch_rebased_kernel<4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    else measure_batch_rebased_kernel<3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+  } else if (cprec == 0) {
     if (ndir == 4) measure_batch_kernel<float, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
     else measure_batch_kernel<float, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
   } else if (gprec == 0) {
@@ -356,6 +413,50 @@ gfx_status run_phase(gfx_batch* b, int prec, int ndir, int ck, double omega, int
   }
   return read_states(b);
 }
+
+// the rebased polish's fields, allocated on first use
+gfx_status ensure_rebased(gfx_batch* b) {
+  size_t ulo = 0;
+  for (int c = 0; c < b->nconf; c++) {
+    BConf& C = b->desc.c[c];
+    C.urstride = (size_t)8 * 3 * C.L.vh;
+    C.w0stride = rebased_w0_bytes(C.L) / 16;
+    ulo = std::max(ulo, C.urstride * 16);
+    gfx_status s;
+    void* p;
+    if (!C.Ur) {
+      if ((s = balloc(b, &p, (size_t)C.ncopies * C.urstride * 16))) return s;
+      C.Ur = p;
+    }
+    if (!C.W0) {
+      if ((s = balloc(b, &p, (size_t)C.ncopies * C.w0stride * 16))) return s;
+      C.W0 = p;
+    }
+  }
+  if (!b->ulo) return balloc(b, &b->ulo, ulo);
+  return GFX_OK;
+}
+
+// copy k of configuration c: a new base from its FP64 g (a = 0), or g = (1 + a) g_c
+void rebase_copy(gfx_batch* b, int c, int k, int ndir) {
+  const BConf& C = b->desc.c[c];
+  launch_rebase(12, ndir, C.L, C.U64, (const double2*)C.G64 + (size_t)k * C.gstride64,
+                (float4*)C.Ur + (size_t)k * C.urstride, b->ulo,
+                (float4*)C.W0 + (size_t)k * C.w0stride, b->stream);
+  cudaMemsetAsync((float4*)C.G32 + (size_t)k * C.gstride32, 0, C.gstride32 * 16, b->stream);
+}
+void compose_copy(gfx_batch* b, int c, int k) {
+  const BConf& C = b->desc.c[c];
+  launch_compose_g(C.L, (double2*)C.G64 + (size_t)k * C.gstride64,
+                   (const float4*)C.G32 + (size_t)k * C.gstride32, b->stream);
+}
+// copy index -> configuration
+int conf_of_copy(const gfx_batch* b, int g) {
+  int c = 0;
+  while (c + 1 < b->nconf && g >= b->desc.c[c + 1].copy_base) c++;
+  return c;
+}
+constexpr int kBatchRebaseSweeps = 1000;  // as the single-lattice polish
 }  // namespace
 
 extern "C" {
@@ -397,6 +498,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
   b->precision = precision;
   b->running = nullptr;
   b->h_states = nullptr;
+  b->ulo = nullptr;
   std::memset((void*)&b->desc, 0, sizeof(b->desc));
   if (stream) {
     b->stream = (cudaStream_t)stream;
@@ -601,7 +703,12 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
     BCK(cudaGetLastError());
   }
   if (handover) {
-    // copies that left the FP32 phase are verified and polished in FP64
+    // copies that left the FP32 phase are verified and polished: with FP64 sweeps, or
+    // (polish = 2) with rebased FP32 sweeps confirmed in FP64, as gfx_overrelax does
+    const bool rebased = p.polish == 2;
+    const int pprec = rebased ? 3 : 1;
+    if (rebased && (s = ensure_rebased(b))) return s;
+    std::vector<char> polished(b->ncopies, 0);
     for (int k = 0; k < b->ncopies; k++) {
       LoopState& H = b->h_states[k];
       iter_switch[k] = H.iter;
@@ -610,15 +717,57 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
         H.done = 0;
         H.prev = 0.0;
         H.ck = p.checkinterval_double;
+        H.rebase_at = rebased ? H.iter + kBatchRebaseSweeps : 0;
+        polished[k] = 1;
+        if (rebased) {
+          const int c = conf_of_copy(b, k);
+          rebase_copy(b, c, k - b->desc.c[c].copy_base, ndir);
+        }
       }
     }
     if ((s = write_states(b))) return s;
-    enqueue_check(b, 1, 1, ndir, 0, 0, 0);
+    enqueue_check(b, pprec, pprec, ndir, 0, 0, 0);
     BCK(cudaGetLastError());
     if ((s = read_states(b))) return s;
-    if (any_running() &&
-        (s = run_phase(b, 1, ndir, p.checkinterval_double, p.omega, p.use_graph)))
-      return s;
+    for (;;) {
+      if (any_running() &&
+          (s = run_phase(b, pprec, ndir, p.checkinterval_double, p.omega, p.use_graph)))
+        return s;
+      if (!rebased) break;
+      // copies due for a new base (done = 5) get one and run on
+      bool again = false;
+      for (int k = 0; k < b->ncopies; k++) {
+        LoopState& H = b->h_states[k];
+        if (H.done != 5) continue;
+        const int c = conf_of_copy(b, k), kc = k - b->desc.c[c].copy_base;
+        compose_copy(b, c, kc);
+        rebase_copy(b, c, kc, ndir);
+        H.done = 0;
+        H.rebase_at = H.iter + kBatchRebaseSweeps;
+        again = true;
+      }
+      if (!again) break;
+      if ((s = write_states(b))) return s;
+    }
+    if (rebased) {
+      // g = (1 + a) g_c in FP64 for every polished copy; an FP64 check confirms the
+      // converged ones, and FP64 sweeps continue where it does not
+      for (int k = 0; k < b->ncopies; k++) {
+        if (!polished[k]) continue;
+        const int c = conf_of_copy(b, k);
+        compose_copy(b, c, k - b->desc.c[c].copy_base);
+        LoopState& H = b->h_states[k];
+        H.rebase_at = 0;
+        if (H.done == 1) H.done = 0;
+      }
+      if ((s = write_states(b))) return s;
+      enqueue_check(b, 1, 1, ndir, 0, 0, 0);
+      BCK(cudaGetLastError());
+      if ((s = read_states(b))) return s;
+      if (any_running() &&
+          (s = run_phase(b, 1, ndir, p.checkinterval_double, p.omega, p.use_graph)))
+        return s;
+    }
   }
   BCK(cudaEventRecord(e1, b->stream));
   BCK(cudaEventSynchronize(e1));

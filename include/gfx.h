@@ -309,7 +309,8 @@ gfx_status gfx_batch_random_haar(gfx_batch *b, uint64_t seed);
 /* fix every copy (one device loop for the whole batch); results[gfx_batch_copies()].
  * Every copy follows exactly the trajectory of gfx_overrelax on a single context with
  * the same parameters, except that the batch uses checkinterval throughout
- * (checkinterval_near is ignored) and polishes with FP64 sweeps (polish is ignored). */
+ * (checkinterval_near is ignored) and polish = 1 polishes with FP64 sweeps as
+ * polish = 0 does (polish = 2, the rebased FP32 sweeps, is supported). */
 gfx_status gfx_batch_overrelax(gfx_batch *b, const gfx_or_params *p, gfx_copy_result *results,
                                double *ms);
 /* the converged copy of configuration conf with the largest functional */

@@ -1,6 +1,7 @@
 """Batched Gribov copies: every copy of every configuration, fixed together in one
 device loop, follows the same trajectory as the same start fixed alone (same check
-iterations, same FP32/FP64 sweep split, same functional to 1e-13)."""
+iterations, same FP32/FP64 sweep split, same functional to 1e-13), with the FP64 and
+with the rebased FP32 polish."""
 import numpy as np
 import pytest
 
@@ -20,11 +21,12 @@ def _batch(gfx, prec, ncopies, seed=900):
     return b, links
 
 
-@pytest.mark.parametrize("prec,ncopies", [(2, [5, 3]), (2, [1, 7]), (0, [3, 2])])
-def test_batch_copies_match_single_contexts(gfx, prec, ncopies):
+@pytest.mark.parametrize("prec,ncopies,polish", [(2, [5, 3], 0), (2, [1, 7], 0), (0, [3, 2], 0),
+                                                 (2, [5, 3], 2)])
+def test_batch_copies_match_single_contexts(gfx, prec, ncopies, polish):
     b, links = _batch(gfx, prec, ncopies)
-    kw = dict(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA,
-              switch_eps=1e-9, checkinterval_double=5)
+    kw = dict(maxit=4000, eps=1e-12 if not polish else 1e-14, checkinterval=20, omega=1.7,
+              criterion=gfx.CRIT_THETA, switch_eps=1e-9, checkinterval_double=5, polish=polish)
     res, ms = b.overrelax(**kw)
     assert all(r["converged"] for r in res)
     base = 0
