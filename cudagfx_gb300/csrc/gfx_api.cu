@@ -1232,18 +1232,28 @@ gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, i
   const int ndir = gauge == GFX_GAUGE_COULOMB ? 3 : 4;
   gfx_status s = prec == 3 ? prepare_rebased(ctx, ndir) : prepare_g(ctx, prec);
   if (s) return s;
+  // the sweeps run as one CUDA graph, back to back as inside the solve's device loop
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  enqueue_sweeps(ctx, prec, ndir, omega, nsweeps);
+  cudaGraph_t graph;
+  CK(cudaStreamEndCapture(ctx->stream, &graph));
+  cudaGraphExec_t exec;
+  cudaError_t ge = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(ge);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaEventRecord(e0, ctx->stream));
-  enqueue_sweeps(ctx, prec, ndir, omega, nsweeps);
+  CK(cudaGraphLaunch(exec, ctx->stream));
   CK(cudaEventRecord(e1, ctx->stream));
   CK(cudaEventSynchronize(e1));
   float t = 0.f;
   CK(cudaEventElapsedTime(&t, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaGraphExecDestroy(exec);
   *ms = t;
   return GFX_OK;
 }

@@ -240,7 +240,8 @@ gfx_status gfx_functional_noalloc(const void *links_device, const void *trafo_de
                                   int ly, int lz, int lt, int link_reals, int gauge,
                                   double *result_device, void *stream);
 
-/* device time (CUDA events on the context's stream) of nsweeps plain OR sweeps */
+/* device time (CUDA events on the context's stream) of nsweeps plain OR sweeps, run
+ * as one CUDA graph (back to back, as in gfx_overrelax's device loop) */
 gfx_status gfx_time_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision,
                            double *ms);
 /* number of kernels this context has enqueued (graph bodies counted per execution) */
