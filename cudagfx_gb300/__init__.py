@@ -102,7 +102,7 @@ class SAParams(_c.Structure):
 
 class ThermParams(_c.Structure):
     _fields_ = [("Nsweep", _c.c_int), ("checkint", _c.c_int), ("beta", _c.c_double),
-                ("variant", _c.c_int)]
+                ("variant", _c.c_int), ("precision", _c.c_int)]
 
 
 class Tuning(_c.Structure):
@@ -454,8 +454,10 @@ class Context:
     def micro_halfsweep(self, parity, gauge=LANDAU, precision=1):
         self._check(lib.gfx_micro_halfsweep(self._h, parity, gauge, precision))
 
-    def thermalize(self, beta, nsweep, checkint=0, variant=HB_REFERENCE):
-        p = ThermParams(nsweep, checkint, beta, variant)
+    def thermalize(self, beta, nsweep, checkint=0, variant=HB_REFERENCE, precision=0):
+        """precision 0: FP64 heatbath (the reference's arithmetic); 1: FP32 staples and
+        SU(2) steps with FP64 reunitarization (SINGLE or MIXED contexts)."""
+        p = ThermParams(nsweep, checkint, beta, variant, precision)
         cap = (nsweep + checkint - 1) // checkint if checkint > 0 else 0
         plaq = np.zeros(max(cap, 1))
         self._check(lib.gfx_thermalize(self._h, _c.byref(p), _ptr(plaq), cap))

@@ -1196,14 +1196,27 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
   if ((long long)kMTCount * ctx->nper_g < 2 * ctx->vol ||
       (long long)kMTCount * ctx->nper_u < 8 * ctx->vol)
     return fail(ctx, GFX_ERR_STATE, "random fields smaller than 2V gauss + 8V uniform");
+  if (p->precision < 0 || p->precision > 1) return fail(ctx, GFX_ERR_ARG, "thermalize precision must be 0 or 1");
+  const bool f32 = p->precision == 1;
+  const int nr32 = ctx->link_nr32;
+  if (f32) {
+    if (!ctx->U32) return fail(ctx, GFX_ERR_STATE, "FP32 thermalization needs a SINGLE or MIXED context");
+    // the FP32 copy in 12 reals while the heatbath keeps it in step with the FP64 links
+    gfx_status s = nr32 != 12 ? set_link_layout32(ctx, 12) : refresh_u32(ctx);
+    if (s) return s;
+  }
   const double beta3 = p->beta / 3.0;
   const int checkint = p->checkint > 0 ? p->checkint : p->Nsweep + 1;
   int np = 0;
   for (int i = 0; i < p->Nsweep; i++) {
     for (int nu = 0; nu < 4; nu++)
       for (int par = 0; par < 2; par++) {
-        launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, par, nu, beta3, ctx->gauss,
-                             ctx->unif, p->variant, 128, ctx->stream);
+        if (f32)
+          launch_link_heatbath_f32(ctx->link_nr, ctx->L, ctx->U64, ctx->U32, par, nu, beta3,
+                                   ctx->gauss, ctx->unif, p->variant, ctx->stream);
+        else
+          launch_link_heatbath(ctx->link_nr, ctx->L, ctx->U64, par, nu, beta3, ctx->gauss,
+                               ctx->unif, p->variant, 128, ctx->stream);
         enqueue_mt_update(ctx);
       }
     if (i % checkint == 0 && plaq && np < plaq_cap) {
@@ -1216,7 +1229,7 @@ gfx_status gfx_thermalize(gfx_ctx* ctx, const gfx_therm_params* p, double* plaq,
   }
   {
     ctx->udf_valid = false;
-    gfx_status rs = refresh_u32(ctx);
+    gfx_status rs = f32 && nr32 != 12 ? set_link_layout32(ctx, nr32) : refresh_u32(ctx);
     if (rs) return rs;
   }
   CK(cudaGetLastError());

@@ -25,11 +25,40 @@ __device__ __forceinline__ int get_a0(double& a0, double kb, float gauss, float4
   return 0;
 }
 
+// dev_heatbath_su2 in FP32 arithmetic, for the FP32 sweeps of g: the same trial,
+// acceptance and construction as below, with the SU(2) parameters formed in float
+// (g is stored in FP32, and GB300's FP64 rate is 1/64 of its FP32 rate, so the FP64
+// form made this kernel FP64-pipe bound)
+__device__ __forceinline__ Su2<float> heatbath_su2_f32(const Su2<float>& w, double beta,
+                                                       float gauss, float4 u) {
+  const float k = fm(w.v[3], w.v[3], fm(w.v[2], w.v[2], fm(w.v[1], w.v[1], w.v[0] * w.v[0])));
+  const float rdet = rsqrtf(k);
+  // dev_get_a0 with y / (k beta) in float
+  const float a = fabsf(gauss);
+  const float y = __fdiv_rn(fm(a, a, -logf(1.0f - u.x)), (float)((double)k * beta));
+  if (!((2.0f * (u.y * u.y)) <= (2.0f - y))) return w;
+  const float a0 = 1.0f - y;
+  const float norm = sqrtf(1.0f - a0 * a0);
+  const float cos_theta = 2.0f * u.z - 1.0f;
+  const float sin_theta = sqrtf(1.0f - cos_theta * cos_theta);
+  float sphi, cphi;
+  sincospif(2.0f * u.w, &sphi, &cphi);
+  const float a1 = norm * sin_theta * cphi, a2 = norm * sin_theta * sphi, a3 = norm * cos_theta;
+  const float v0 = w.v[0] * rdet, v1 = w.v[1] * rdet, v2 = w.v[2] * rdet, v3 = w.v[3] * rdet;
+  Su2<float> al;
+  al.v[0] = a0 * v0 - a1 * v1 - a2 * v2 - a3 * v3;
+  al.v[1] = a0 * v1 + a1 * v0 - a2 * v3 + a3 * v2;
+  al.v[2] = a0 * v2 + a2 * v0 - a3 * v1 + a1 * v3;
+  al.v[3] = a0 * v3 + a3 * v0 - a1 * v2 + a2 * v1;
+  return al;
+}
+
 // dev_heatbath_su2 (simulated_annealing.cu:33-73).  k = |w|^2 as in the reference;
 // on rejection alpha = w (unnormalized), which the final reunitarization absorbs.
 template <typename T>
 __device__ __forceinline__ Su2<T> heatbath_su2(const Su2<T>& wt, double beta, float gauss,
                                                float4 u) {
+  if constexpr (sizeof(T) == 4) return heatbath_su2_f32(wt, beta, gauss, u);
   double w[4] = {(double)wt.v[0], (double)wt.v[1], (double)wt.v[2], (double)wt.v[3]};
   const double k = w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + w[3] * w[3];
   const double rdet = rsqrt(k);
@@ -110,6 +139,33 @@ __device__ __forceinline__ Su2<T> heatbath_su2_kp(const Su2<T>& wt, double beta,
   al.v[1] = (T)(a[0] * v[1] + a[1] * v[0] - a[2] * v[3] + a[3] * v[2]);
   al.v[2] = (T)(a[0] * v[2] + a[2] * v[0] - a[3] * v[1] + a[1] * v[3]);
   al.v[3] = (T)(a[0] * v[3] + a[3] * v[0] - a[1] * v[2] + a[2] * v[1]);
+  return al;
+}
+
+// the same Kennedy-Pendleton trial in FP32 arithmetic (the FP32 thermalization)
+__device__ __forceinline__ Su2<float> heatbath_su2_kp_f32(const Su2<float>& w, double beta,
+                                                          float gauss, float4 u) {
+  const float k = sqrtf(fm(w.v[3], w.v[3], fm(w.v[2], w.v[2], fm(w.v[1], w.v[1], w.v[0] * w.v[0]))));
+  Su2<float> al;
+  al.v[0] = 1.f;
+  al.v[1] = al.v[2] = al.v[3] = 0.f;
+  if (!(k > 0.f)) return al;
+  const float rk = 1.f / k;
+  const float E = -logf(1.f - u.x);
+  const float y = __fdiv_rn(fm(0.5f * gauss, gauss, E), (float)beta * k);
+  if (!(u.y * u.y <= 1.f - 0.5f * y)) return al;
+  const float a0 = 1.f - y;
+  const float norm = sqrtf(fmaxf(0.f, 1.f - a0 * a0));
+  const float cos_theta = 2.f * u.z - 1.f;
+  const float sin_theta = sqrtf(fmaxf(0.f, 1.f - cos_theta * cos_theta));
+  float sphi, cphi;
+  sincospif(2.f * u.w, &sphi, &cphi);
+  const float a1 = norm * sin_theta * cphi, a2 = norm * sin_theta * sphi, a3 = norm * cos_theta;
+  const float v0 = w.v[0] * rk, v1 = w.v[1] * rk, v2 = w.v[2] * rk, v3 = w.v[3] * rk;
+  al.v[0] = a0 * v0 - a1 * v1 - a2 * v2 - a3 * v3;
+  al.v[1] = a0 * v1 + a1 * v0 - a2 * v3 + a3 * v2;
+  al.v[2] = a0 * v2 + a2 * v0 - a3 * v1 + a1 * v3;
+  al.v[3] = a0 * v3 + a3 * v0 - a1 * v2 + a2 * v1;
   return al;
 }
 
@@ -291,6 +347,99 @@ __global__ void __launch_bounds__(128) link_heatbath_kernel(Lattice L, double2* 
   }
   normalize<double, true>(link);
   Field<double, NR>::store(blk, (size_t)L.vh, i, link);
+}
+
+// The same update in FP32 arithmetic, for thermalization: staples from the FP32 link
+// copy (12 reals), the SU(2) heatbath steps on an FP32 copy of the link, then the new
+// link is reunitarized in FP64 and stored in both copies, so they stay in step.  A
+// heatbath draws the new link at random; FP32 arithmetic moves the drawn link by
+// ~1e-7, far below the spread of the draw, so the chain samples the same
+// distribution, while the kernel runs on the FP32 units instead of the FP64 pipe.
+__device__ __forceinline__ void ld_link32(const Lattice& L, const float4* __restrict__ U32,
+                                          Coord c, int mu, Mat3<float>& m) {
+  const int p = (c.x + c.y + c.z + c.t) & 1;
+  const int i = (c.x >> 1) + L.lxh * (c.y + L.ly * (c.z + L.lz * c.t));
+  Field<float, 12>::load(U32 + (size_t)(p * 4 + mu) * 3 * L.vh, (size_t)L.vh, i, m);
+}
+
+template <int NR, int VARIANT>
+__global__ void __launch_bounds__(128) link_heatbath_f32_kernel(Lattice L, double2* U,
+                                                                 float4* U32, int parity, int nu,
+                                                                 double beta3, const float* gauss,
+                                                                 const float4* unif4) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= L.vh) return;
+  const Site s = site_of(L, i, parity);
+  const Coord x = {2 * s.xh + s.s, s.y, s.z, s.t};
+  Mat3<float> staple, h1, h2, h3;
+  mzero(staple);
+#pragma unroll
+  for (int mu = 0; mu < 4; mu++) {
+    if (mu == nu) continue;
+    const Coord xpn = cshift(L, x, nu, 1);
+    const Coord xpm = cshift(L, x, mu, 1);
+    const Coord xmm = cshift(L, x, mu, -1);
+    const Coord xpnmm = cshift(L, xpn, mu, -1);
+    // U_mu(x+nu) U_nu^+(x+mu) U_mu^+(x)
+    ld_link32(L, U32, xpn, mu, h1);
+    ld_link32(L, U32, xpm, nu, h2);
+    mzero(h3);
+    addmul_nd(h3, h1, h2);
+    ld_link32(L, U32, x, mu, h1);
+    addmul_nd(staple, h3, h1);
+    // U_mu^+(x+nu-mu) U_nu^+(x-mu) U_mu(x-mu)
+    ld_link32(L, U32, xpnmm, mu, h1);
+    ld_link32(L, U32, xmm, nu, h2);
+    mzero(h3);
+    addmul_dd(h3, h1, h2);
+    ld_link32(L, U32, xmm, mu, h1);
+    addmul(staple, h3, h1);
+  }
+  Mat3<float> link;
+  ld_link32(L, U32, x, nu, link);
+  if (VARIANT == 0) {
+    const int r = 4 * i + nu;
+    cm_heatbath(link, staple, beta3, __ldg(gauss + r), __ldg(unif4 + r));
+  } else {
+#pragma unroll
+    for (int sg = 0; sg < 3; sg++) {
+      const int r = 4 * i + ((nu + sg) & 3);
+      const int a = sub_a(sg), b = sub_b(sg);
+      Su2<float> w = su2_extract(link, staple, a, b);
+      su2_rotate(link, a, b, heatbath_su2_kp_f32(w, beta3, __ldg(gauss + r), __ldg(unif4 + r)));
+    }
+  }
+  Mat3<double> ld;
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) ld.e[r][c] = cmk<double>(link.e[r][c].re, link.e[r][c].im);
+  normalize<double, true>(ld);
+  constexpr int NC = Field<double, NR>::NCHUNK;
+  Field<double, NR>::store(U + (size_t)(parity * 4 + nu) * NC * L.vh, (size_t)L.vh, i, ld);
+#pragma unroll
+  for (int r = 0; r < 2; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      link.e[r][c] = cmk<float>((float)ld.e[r][c].re, (float)ld.e[r][c].im);
+  Field<float, 12>::store(U32 + (size_t)(parity * 4 + nu) * 3 * L.vh, (size_t)L.vh, i, link);
+}
+
+void launch_link_heatbath_f32(int link_nr, const Lattice& L, void* U, void* U32, int parity,
+                              int nu, double beta3, const float* gauss, const float* unif,
+                              int variant, cudaStream_t s) {
+  dim3 grid((L.vh + 127) / 128);
+#define LHB32(NR, VAR)                                                                      \
+  link_heatbath_f32_kernel<NR, VAR><<<grid, 128, 0, s>>>(L, (double2*)U, (float4*)U32, parity, \
+                                                         nu, beta3, gauss, (const float4*)unif)
+  if (link_nr == 18) {
+    if (variant) LHB32(18, 1);
+    else LHB32(18, 0);
+  } else {
+    if (variant) LHB32(12, 1);
+    else LHB32(12, 0);
+  }
+#undef LHB32
 }
 
 void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu, double beta3,

@@ -104,6 +104,10 @@ void launch_micro(int prec, int link_nr, int ndir, const Lattice& L, const void*
 void launch_link_heatbath(int link_nr, const Lattice& L, void* U, int parity, int nu,
                           double beta3, const float* gauss, const float* unif, int variant,
                           int block, cudaStream_t s);
+// the same in FP32 arithmetic from the 12-real FP32 copy U32, updating U and U32
+void launch_link_heatbath_f32(int link_nr, const Lattice& L, void* U, void* U32, int parity,
+                              int nu, double beta3, const float* gauss, const float* unif,
+                              int variant, cudaStream_t s);
 
 // ----- Mersenne Twister bank (gfx_mt.cu) -----
 struct MTBank {

@@ -245,6 +245,7 @@ void thermalize_gauge(void) {
   tp.checkint = 0;
   tp.beta = thermparam.beta;
   tp.variant = GFX_HB_REFERENCE;
+  tp.precision = 0;
   const int ck = thermparam.checkint > 0 ? thermparam.checkint : 1;
   for (int i = 0; i < thermparam.Nsweep; i++) {
     if (gfx_thermalize(g_ctx, &tp, nullptr, 0) != GFX_OK) {
