@@ -79,6 +79,9 @@ def parse():
                     help="skip the batched-Gribov-copies measurement")
     ap.add_argument("--gribov-copies", default="64,32",
                     help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
+    ap.add_argument("--config", choices=["c3", "c5"], default=None,
+                    help="instead of the bench: the full 32^4 Coulomb (c3) or 48^3x96 (c5) "
+                         "workload, mixed against all-FP64 (--no-fp64 skips that solve)")
     ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2],
                     help="--kernels: OR half-sweep staging mode")
     ap.add_argument("--kernels", action="store_true",
@@ -148,7 +151,8 @@ def gribov_batch(args, gfx, mt_source):
 def run_kernels(args, dims):
     """A short fixed workload for profiler captures: 3 FP32 OR sweeps, an FP32 and an
     FP64 functional, 1 FP64 OR sweep, 3 rebased FP32 sweeps and their functional, one
-    SA step and one link-heatbath sweep.  The OR sweeps use --staging (2, the tuner's
+    SA step with one microcanonical step, and one link-heatbath sweep in FP64 and one in
+    FP32 arithmetic.  The OR sweeps use --staging (2, the tuner's
     choice on 32^4: the odd half-sweep in reverse block order)."""
     import cudagfx_gb300 as gfx
     V = int(np.prod(dims))
@@ -170,8 +174,9 @@ def run_kernels(args, dims):
         ctx.mt_load_params(synthetic_mt_params())
     ctx.mt_seed(42)
     ctx.mt_init(2 * V, 8 * V)
-    ctx.simanneal(0.5, 0.5, 1)
+    ctx.simanneal(0.5, 0.5, 1, nmicro=1)
     ctx.thermalize(args.beta, 1, variant=gfx.HB_KENNEDY_PENDLETON)
+    ctx.thermalize(args.beta, 1, variant=gfx.HB_KENNEDY_PENDLETON, precision=1)
     ctx.close()
     print("kernels ok")
 
@@ -569,10 +574,85 @@ def run_gfx(args, dims):
     print(json.dumps(out), flush=True)
 
 
+def run_config(args):
+    """The full C3 or C5 workload on one GPU, one JSON line:
+    c3  32^4 beta 6.0 (200 FP64 KP heatbath sweeps from cold, MT seed 42), Coulomb
+        gauge from the reference random start (RandSeed 351) to theta_t < 1e-15 per
+        slice, mixed (rebased polish) against all-FP64, plaquette and Polyakov loop
+        before and after fixing;
+    c5  48^3x96 beta 6.2, FP64 18-real links: 1000 FP32-arithmetic KP heatbath sweeps
+        from cold (MT seed 2024), SA 1000 steps T 1.0 -> 0.01 with 3 microcanonical
+        steps each, then Landau OR omega 1.7 to theta < 1e-14, mixed (rebased polish)
+        against all-FP64 from the same annealed g."""
+    import cudagfx_gb300 as gfx
+    from cudagfx_gb300 import build as b
+    b.build()
+    c5 = args.config == "c5"
+    dims = (48, 48, 48, 96) if c5 else (32, 32, 32, 32)
+    V = int(np.prod(dims))
+    out = {"config": args.config, "lattice": list(dims)}
+
+    def now(c):
+        c.synchronize()
+        return time.perf_counter()
+
+    c = gfx.Context(dims, precision=gfx.PREC_MIXED, link_reals=18 if c5 else 12)
+    c.set_links(gfx.unit_init(4 * V))
+    dat = mt_params_path()
+    c.mt_load_file(dat) if dat else c.mt_load_params(synthetic_mt_params())
+    c.mt_seed(2024 if c5 else 42)
+    c.mt_init(2 * V, 8 * V)
+    t0 = now(c)
+    c.thermalize(6.2 if c5 else 6.0, 1000 if c5 else 200, variant=gfx.HB_KENNEDY_PENDLETON,
+                 precision=1 if c5 else 0)
+    out["thermalize_s"] = now(c) - t0
+    plaq0, poly0 = c.plaquette(), c.polyakov()
+    out["plaquette"] = plaq0
+    c.set_trafo(gfx.random_init_reference(351, V))
+    if c5:
+        t0 = now(c)
+        c.simanneal(0.01, 1.0, 1000, expo=-1.0, checkint=1000, nmicro=3)
+        out["simanneal_s"] = now(c) - t0
+        kw = dict(maxit=20000, eps=1e-14, checkinterval=100, omega=1.7,
+                  criterion=gfx.CRIT_THETA, checkinterval_near=10)
+        gauge = gfx.LANDAU
+    else:
+        kw = dict(maxit=20000, eps=1e-15, checkinterval=50, omega=1.7, gauge=gfx.COULOMB,
+                  criterion=gfx.CRIT_THETA_SLICES)
+        gauge = gfx.COULOMB
+    g_start = c.get_trafo()
+    r = c.overrelax(polish=2, **kw)
+    f = c.functional(gauge=gauge)
+    out["mixed"] = {"s": r.ms / 1000.0, "converged": r.converged, "sweeps_fp32": r.sweeps_single,
+                    "sweeps_polish": r.sweeps_double, "theta": f.theta,
+                    "theta_slice_max": f.theta_slice_max, "F": f.F}
+    g_mixed = c.get_trafo()
+    links = c.get_links() if not args.no_fp64 else None
+    c.apply_trafo()
+    out["plaquette_rel_change"] = abs(c.plaquette() - plaq0) / plaq0
+    out["polyakov_abs_change"] = abs(c.polyakov() - poly0)
+    c.close()
+    if not args.no_fp64:
+        d = gfx.Context(dims, precision=gfx.PREC_DOUBLE, link_reals=18 if c5 else 12)
+        d.set_links(links)
+        d.set_trafo(g_start)
+        r64 = d.overrelax(**kw)
+        f64 = d.functional(gauge=gauge)
+        out["fp64"] = {"s": r64.ms / 1000.0, "converged": r64.converged, "sweeps": r64.sweeps,
+                       "theta": f64.theta, "theta_slice_max": f64.theta_slice_max, "F": f64.F}
+        out["speedup"] = r64.ms / r.ms
+        out["F_mixed_minus_fp64"] = f.F - f64.F
+        out["max_abs_g_diff"] = float(np.max(np.abs(g_mixed - d.get_trafo())))
+        d.close()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     dims = tuple(int(x) for x in args.dims.split(","))
-    if args.kernels:
+    if args.config:
+        run_config(args)
+    elif args.kernels:
         run_kernels(args, dims)
     elif args.impl == "reference":
         run_reference(args, dims)
