@@ -209,10 +209,13 @@ def _mt_ctx(gfx, mt_params, seed, ng, nu, dims=(4, 4, 4, 4)):
     return ctx
 
 
-@pytest.mark.parametrize("ng,nu", [(4096 * 38, 4096 * 19), (4096 * 6, 4096 * 24), (5000, 70001)])
+@pytest.mark.parametrize("ng,nu", [(4096 * 38, 4096 * 19), (4096 * 6, 4096 * 24), (5000, 70001),
+                                   (4096 * 160, 4096 * 311)])
 def test_mt_bank_bit_exact(gfx, oracle, mt_params, ng, nu):
     """Uniform fields and the twister state are bit-exact with the oracle through init
-    and three updates; gaussians (fast-math Box-Muller) agree to 2e-4 absolute."""
+    and three updates; gaussians (fast-math Box-Muller) agree to 2e-4 absolute.  The
+    sizes cover partial rounds of the 19-word ring and, with 160 and 312 outputs per
+    twister, the generator's 152-output tiles."""
     ctx = _mt_ctx(gfx, mt_params, 1234, ng, nu)
     npg, npu = ctx.mt_sizes()
     assert (npg, npu) == (oracle.mt_nper(ng), oracle.mt_nper(nu))
