@@ -79,9 +79,10 @@ def parse():
                     help="skip the batched-Gribov-copies measurement")
     ap.add_argument("--gribov-copies", default="64,32",
                     help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
-    ap.add_argument("--config", choices=["c3", "c5"], default=None,
-                    help="instead of the bench: the full 32^4 Coulomb (c3) or 48^3x96 (c5) "
-                         "workload, mixed against all-FP64 (--no-fp64 skips that solve)")
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c5"], default=None,
+                    help="instead of the bench: one full workload, mixed against all-FP64 "
+                         "(--no-fp64 skips that solve): c1 8^4 (also on the CPU oracle), c2 "
+                         "16^3x32 SA then OR, c3 32^4 Coulomb, c5 48^3x96")
     ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2],
                     help="--kernels: OR half-sweep staging mode")
     ap.add_argument("--kernels", action="store_true",
@@ -574,6 +575,77 @@ def run_gfx(args, dims):
     print(json.dumps(out), flush=True)
 
 
+def run_config_small(args):
+    """c1  8^4 beta 6.0, links from the reference's heatbath (200 sweeps from cold, MT
+        seed 1234), reference random gauge start (RandSeed 351), Landau OR omega 1.7
+        to theta < 1e-12: mixed and all-FP64 on the GPU, and as the CPU baseline the
+        oracle's FP64 port of the reference loop on the host cores (checks every 100
+        sweeps);
+    c2  16^3x32 beta 6.0 (500 KP heatbath sweeps, MT seed 7): SA 2000 steps T 1.45 ->
+        0.01 (linear) with 3 microcanonical steps each on FP32 g, then OR omega 1.7 to
+        theta < 1e-12, mixed against all-FP64 from the same annealed g."""
+    import cudagfx_gb300 as gfx
+    from cudagfx_gb300 import build as b
+    b.build()
+    c1 = args.config == "c1"
+    dims = (8, 8, 8, 8) if c1 else (16, 16, 16, 32)
+    V = int(np.prod(dims))
+    out = {"config": args.config, "lattice": list(dims)}
+    c = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    c.set_links(gfx.unit_init(4 * V))
+    dat = mt_params_path()
+    c.mt_load_file(dat) if dat else c.mt_load_params(synthetic_mt_params())
+    c.mt_seed(1234 if c1 else 7)
+    c.mt_init(2 * V, 8 * V)
+    c.thermalize(6.0, 200 if c1 else 500,
+                 variant=gfx.HB_REFERENCE if c1 else gfx.HB_KENNEDY_PENDLETON)
+    out["plaquette"] = c.plaquette()
+    links = c.get_links()
+    c.set_trafo(gfx.random_init_reference(351, V))
+    if not c1:
+        c.synchronize()
+        t0 = time.perf_counter()
+        c.simanneal(0.01, 1.45, 2000, expo=-1.0, checkint=2000, nmicro=3)
+        c.synchronize()
+        out["simanneal_s"] = time.perf_counter() - t0
+    g_start = c.get_trafo()
+    kw = dict(maxit=20000, eps=1e-12, checkinterval=100 if c1 else 50, omega=1.7,
+              criterion=gfx.CRIT_THETA)
+    r = c.overrelax(polish=2, **kw)
+    f = c.functional()
+    out["mixed"] = {"s": r.ms / 1000.0, "converged": r.converged, "sweeps_fp32": r.sweeps_single,
+                    "sweeps_polish": r.sweeps_double, "theta": f.theta, "F": f.F}
+    c.close()
+    if not args.no_fp64:
+        d = gfx.Context(dims, precision=gfx.PREC_DOUBLE)
+        d.set_links(links)
+        d.set_trafo(g_start)
+        r64 = d.overrelax(**kw)
+        f64 = d.functional()
+        out["fp64"] = {"s": r64.ms / 1000.0, "converged": r64.converged, "iterations": r64.iterations,
+                       "sweeps": r64.sweeps, "theta": f64.theta, "F": f64.F}
+        out["F_mixed_minus_fp64"] = f.F - f64.F
+        d.close()
+    if c1:
+        import oracle as orc
+        o = orc.Oracle()
+        lat = o.lattice(dims)
+        gf12, g12 = o.to2v(links), np.ascontiguousarray(np.asarray(g_start).reshape(-1, 18)[:, :12])
+        t0 = time.perf_counter()
+        it = 0
+        o.or_sweeps(lat, gf12, g12, 1, 1.7)
+        fo = o.functional(lat, gf12, g12)
+        while fo["dAdA"] / 3.0 >= kw["eps"] and it < kw["maxit"]:
+            o.or_sweeps(lat, gf12, g12, kw["checkinterval"], 1.7)
+            it += kw["checkinterval"]
+            fo = o.functional(lat, gf12, g12)
+        # the CPU baseline of this workload: the oracle's port of the reference update
+        out["cpu_baseline"] = {"kind": "port", "s": time.perf_counter() - t0, "iterations": it,
+                               "theta": fo["dAdA"] / 3.0, "F": fo["F"],
+                               "cores": os.cpu_count()}
+    print(json.dumps(out))
+
+
 def run_config(args):
     """The full C3 or C5 workload on one GPU, one JSON line:
     c3  32^4 beta 6.0 (200 FP64 KP heatbath sweeps from cold, MT seed 42), Coulomb
@@ -650,7 +722,9 @@ def run_config(args):
 def main():
     args = parse()
     dims = tuple(int(x) for x in args.dims.split(","))
-    if args.config:
+    if args.config in ("c1", "c2"):
+        run_config_small(args)
+    elif args.config:
         run_config(args)
     elif args.kernels:
         run_kernels(args, dims)
