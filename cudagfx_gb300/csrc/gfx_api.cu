@@ -780,7 +780,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
     if (H.done == 0) {
       const int it0 = H.iter;
       if (p.use_graph) {
-        cudaGraphExec_t ex;
+        cudaGraphExec_t ex = nullptr;
         s = get_graph(ctx, prec, ndir, H.ck, p.omega, &ex);
         if (s) return s;
         const unsigned long long before = ctx->launches;

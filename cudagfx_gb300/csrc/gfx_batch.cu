@@ -73,7 +73,6 @@ __device__ __forceinline__ int conf_of(const BDesc& d, int item, int BConf::*bas
 template <typename T, int NDIR>
 __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_kernel(BDesc d, int parity, T omega) {
   typedef typename VecOf<T>::type V;
-  constexpr int NC = Field<T, 12>::NCHUNK;
   // parity 1 runs the work items in reverse order: it starts on the ranges parity 0
   // touched last, which L2 may still hold (the order does not change any result)
   const int item = parity ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;

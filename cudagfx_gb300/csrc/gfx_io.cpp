@@ -469,7 +469,7 @@ gfx_status gfx_bqcd_read_info(const char* path, gfx_bqcd_info* info, gfx_slice_c
       unsigned long long sum, bytes;
       if (std::sscanf(line, "%255s %llu %llu", file, &sum, &bytes) == 3) {
         if (cks && n < cap) {
-          std::snprintf(cks[n].file, sizeof(cks[n].file), "%s", file);
+          std::snprintf(cks[n].file, sizeof(cks[n].file), "%.79s", file);  // the field's width
           cks[n].sum = sum;
           cks[n].bytes = bytes;
         }

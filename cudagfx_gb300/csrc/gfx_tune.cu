@@ -203,7 +203,8 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
       if ((s = prepare_g(ctx, prec))) break;
       if (n == 0) {
         double t1 = 0.0;
-        if ((s = time_reps(ctx, 2, [&]() { enqueue_sweep(ctx, prec, ndir, 1.7); }, &t1))) break;
+        s = time_reps(ctx, 2, [&]() { enqueue_sweep(ctx, prec, ndir, 1.7); }, &t1);
+        if (s) break;
         n = std::min(40, std::max(2, (int)std::ceil(3.0 / std::max(t1, 1e-3))));
       }
       auto sweep = [&]() { enqueue_sweeps(ctx, prec, ndir, 1.7, n); };
