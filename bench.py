@@ -505,6 +505,7 @@ def run_gfx(args, dims):
         r64 = solve(c64, p64)
         t_fp64 = r64.ms / 1000.0
         sweeps64 = r64.sweeps
+        fv64 = r64.final_values
         c64.close()
     hbm, peak_kind = measured_peaks()
     t32_share = r_last.sweeps_single * 2 * ms32
@@ -563,7 +564,12 @@ def run_gfx(args, dims):
                              "polish_rebased_fp32": r_last.sweeps_polish_fp32},
         "time_to_theta_s": {"mixed": r_last.ms / 1000.0, "fp64": t_fp64,
                             "fp64_sweeps": sweeps64,
-                            "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None},
+                            "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None,
+                            # both measured in FP64 at the end of their solves
+                            "theta_mixed": r_last.final_values.theta,
+                            "theta_fp64": fv64.theta if t_fp64 else None,
+                            "F_mixed_minus_fp64": (r_last.final_values.F - fv64.F) if t_fp64
+                            else None},
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
