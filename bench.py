@@ -470,7 +470,7 @@ def run_gfx(args, dims):
     pin_g0 = gfx.pinned_empty(g0.shape)
     pin_g0[...] = g0
     pin_out = gfx.pinned_empty(g0.shape)
-    e2e_t, e2e_upd = 0.0, 0
+    e2e_t, e2e_upd, e2e_dev = 0.0, 0, 0.0
     for _ in range(args.steps):
         ctx.synchronize()
         t0 = time.perf_counter()
@@ -480,6 +480,7 @@ def run_gfx(args, dims):
         ctx.get_trafo_into(pin_out)
         e2e_t += time.perf_counter() - t0
         e2e_upd += r.sweeps * V
+        e2e_dev += r.ms / 1000.0
     e2e_t = max_over_ranks(dist, e2e_t)
     e2e_value = e2e_upd * ws / e2e_t
 
@@ -573,7 +574,9 @@ def run_gfx(args, dims):
         "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": pin_out.nbytes},
+                "d2h_bytes_per_step": pin_out.nbytes,
+                # wall time per step, and the solve's device time within it
+                "s_per_step": e2e_t / args.steps, "solve_device_s_per_step": e2e_dev / args.steps},
         "clocks": clocks,
         "gpu_launches": int(launches),
         "gribov_batch": gribov,
