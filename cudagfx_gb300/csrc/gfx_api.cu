@@ -748,7 +748,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   LoopState& H = *ctx->loop_host;
   std::memset(&H, 0, sizeof(H));
   H.iter = 0;
-  // checkinterval_double applies to the FP64 polish after a mixed-precision handover;
+  // checkinterval_double applies to the polish after a mixed-precision handover;
   // a single-precision-mode run checks every checkinterval sweeps (overrelax.cu:775)
   H.ck = p.checkinterval;
   H.ck_near = p.checkinterval_near;
@@ -836,8 +836,9 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       continue;
     }
     if (H.done == 2) {
-      // FP32 phase finished: widen g (reunitarized in FP64), then polish in FP64 or
-      // double-float; the first check verifies the handover state
+      // FP32 phase finished: widen g (reunitarized in FP64), then polish in FP64,
+      // double-float or rebased FP32 (a new base from the widened g); the first check
+      // verifies the handover state
       s = prepare_g(ctx, 1);
       if (s) return s;
       prec = p.polish == 2 ? 3 : p.polish == 1 ? 2 : 1;

@@ -120,10 +120,11 @@ gfx_status ensure_scratch(gfx_ctx* ctx, size_t bytes);
 void destroy_graphs(gfx_ctx* ctx);
 // the FP32 link copy from the FP64 links, in the current FP32 layout
 gfx_status refresh_u32(gfx_ctx* ctx);
-// make G64 the current g (from G32 or Gdf)
+// make G64 the current g (from G32, from Gdf, or composed as (1 + a) G64 on a rebased base)
 gfx_status sync_g64(gfx_ctx* ctx);
 gfx_status ensure_df(gfx_ctx* ctx);
-// make the g of precision prec (0 FP32, 1 FP64, 2 double-float) the current one
+// make the g of precision prec (0 FP32, 1 FP64, 2 double-float) the current one; the
+// rebased FP32 state comes from prepare_rebased
 gfx_status prepare_g(gfx_ctx* ctx, int prec);
 // a new base for the rebased FP32 sweeps over ndir directions: g_c = g, a = 0
 gfx_status rebase(gfx_ctx* ctx, int ndir);
