@@ -108,7 +108,9 @@ __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
                                                        const typename VecOf<TSU>::type* U,
                                                        const typename VecOf<TSG>::type* G,
                                                        double* partials) {
-  const int parity = blockIdx.z, t = blockIdx.y;
+  // parity is the inner grid dimension: both parities of a slice run back to back, so
+  // the links and g they share are read from L2 the second time
+  const int parity = blockIdx.y, t = blockIdx.z;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   double f = 0.0, d = 0.0;
   if (k < L.st) {
@@ -128,7 +130,7 @@ int measure_blocks_x(const Lattice& L, int block) { return (L.st + block - 1) / 
 
 void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
                     const void* G, double* partials, int block, cudaStream_t s) {
-  dim3 grid(measure_blocks_x(L, block), L.lt, 2);
+  dim3 grid(measure_blocks_x(L, block), 2, L.lt);
 #define MEAS(TC, TSU, NR, TSG, ND)                                                    \
   measure_kernel<TC, TSU, NR, TSG, ND><<<grid, block, 0, s>>>(                      \
       L, (const typename VecOf<TSU>::type*)U, (const typename VecOf<TSG>::type*)G, \

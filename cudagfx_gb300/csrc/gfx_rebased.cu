@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(256) measure_rebased_kernel(Lattice L,
                                                               const float4* __restrict__ W0,
                                                               const float4* __restrict__ A,
                                                               double* partials) {
-  const int parity = blockIdx.z, t = blockIdx.y;
+  const int parity = blockIdx.y, t = blockIdx.z;  // parity inner, as measure_kernel
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   double f = 0.0, d = 0.0;
   if (k < L.st) {
@@ -229,7 +229,7 @@ void launch_or_rebased(int ndir, const Lattice& L, const void* Ur, const void* W
 
 void launch_measure_rebased(int ndir, const Lattice& L, const void* Ur, const void* W0,
                             const void* A, double* partials, int block, cudaStream_t s) {
-  const dim3 g(measure_blocks_x(L, block), L.lt, 2);
+  const dim3 g(measure_blocks_x(L, block), 2, L.lt);
   if (ndir == 4)
     measure_rebased_kernel<4><<<g, block, 0, s>>>(L, (const float4*)Ur, (const float4*)W0,
                                                   (const float4*)A, partials);
