@@ -568,6 +568,7 @@ def run_gfx(args, dims):
                             "speedup": (t_fp64 / (r_last.ms / 1000.0)) if t_fp64 else None,
                             # both measured in FP64 at the end of their solves
                             "theta_mixed": r_last.final_values.theta,
+                            "maxdAdA_mixed": r_last.final_values.maxdAdA,  # the reference's criterion
                             "theta_fp64": fv64.theta if t_fp64 else None,
                             "F_mixed_minus_fp64": (r_last.final_values.F - fv64.F) if t_fp64
                             else None},
