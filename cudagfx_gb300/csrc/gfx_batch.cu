@@ -437,12 +437,14 @@ gfx_status ensure_rebased(gfx_batch* b) {
 }
 
 // copy k of configuration c: a new base from its FP64 g (a = 0), or g = (1 + a) g_c
-void rebase_copy(gfx_batch* b, int c, int k, int ndir) {
+gfx_status rebase_copy(gfx_batch* b, int c, int k, int ndir) {
   const BConf& C = b->desc.c[c];
   launch_rebase(12, ndir, C.L, C.U64, (const double2*)C.G64 + (size_t)k * C.gstride64,
                 (float4*)C.Ur + (size_t)k * C.urstride, b->ulo,
                 (float4*)C.W0 + (size_t)k * C.w0stride, b->stream);
-  cudaMemsetAsync((float4*)C.G32 + (size_t)k * C.gstride32, 0, C.gstride32 * 16, b->stream);
+  BCK(cudaGetLastError());
+  BCK(cudaMemsetAsync((float4*)C.G32 + (size_t)k * C.gstride32, 0, C.gstride32 * 16, b->stream));
+  return GFX_OK;
 }
 void compose_copy(gfx_batch* b, int c, int k) {
   const BConf& C = b->desc.c[c];
@@ -720,7 +722,7 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
         polished[k] = 1;
         if (rebased) {
           const int c = conf_of_copy(b, k);
-          rebase_copy(b, c, k - b->desc.c[c].copy_base, ndir);
+          if ((s = rebase_copy(b, c, k - b->desc.c[c].copy_base, ndir))) return s;
         }
       }
     }
@@ -740,7 +742,7 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
         if (H.done != 5) continue;
         const int c = conf_of_copy(b, k), kc = k - b->desc.c[c].copy_base;
         compose_copy(b, c, kc);
-        rebase_copy(b, c, kc, ndir);
+        if ((s = rebase_copy(b, c, kc, ndir))) return s;
         H.done = 0;
         H.rebase_at = H.iter + kBatchRebaseSweeps;
         again = true;
