@@ -91,15 +91,48 @@ def parse():
     return ap.parse_args()
 
 
-def gribov_batch(args, gfx, mt_source):
+def split_copies(ncopies, rank, ws):
+    """The Gribov copies rank `rank` of `ws` fixes: copies r, r + ws, r + 2 ws, ... of
+    every configuration (indices within the configuration).  Copies are independent,
+    so the replicas share no data during the solve."""
+    return [list(range(rank, n, ws)) for n in ncopies]
+
+
+def gather_best(dist, ws, local):
+    """local[k] = (F, copy) of this rank's best converged copy of configuration k, or
+    None; returns the best over all ranks (largest F, then the lower copy index)."""
+    if dist is None or ws == 1:
+        return list(local)
+    every = [None] * ws
+    dist.all_gather_object(every, list(local))
+    best = []
+    for k in range(len(local)):
+        cand = [r[k] for r in every if r[k] is not None]
+        best.append(max(cand, key=lambda fc: (fc[0], -fc[1])) if cand else None)
+    return best
+
+
+def sum_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=_coll_device())
+    dist.all_reduce(t)
+    return float(t.item())
+
+
+def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
     """Batched Gribov copies: 64 copies of a 16^4 beta=6.0 configuration and 32 copies of
     a 24^4 beta=6.2 configuration, Haar-random starts (seed 2024 + copy), mixed OR
     omega=1.7 (FP32, then the --polish sweeps; double-float is not batched and falls
     back to FP64) to theta<1e-12, the largest-functional copy kept per configuration.
     Batched: one device loop for all copies.  Sequential: the same starts, one
-    single-lattice solve per copy.  Both timed with CUDA events (solve only)."""
+    single-lattice solve per copy.  Both timed with CUDA events (solve only).  Under
+    N ranks each rank fixes copies r, r + N, ... (split_copies); the times are the
+    slowest rank's and the best copy is gathered over the ranks."""
     confs = [((16, 16, 16, 16), 6.0), ((24, 24, 24, 24), 6.2)]
     ncopies = [int(x) for x in args.gribov_copies.split(",")]
+    mine = split_copies(ncopies, rank, ws)
     kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval or 25, omega=args.omega,
               criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
               checkinterval_double=args.checkinterval_double,
@@ -115,38 +148,55 @@ def gribov_batch(args, gfx, mt_source):
         c.thermalize(beta, args.therm, variant=gfx.HB_KENNEDY_PENDLETON)
         links.append(c.get_links())
         c.close()
-    b = gfx.Batch([d for d, _ in confs], ncopies, precision=gfx.PREC_MIXED)
-    for k, u in enumerate(links):
-        b.set_links(k, u)
-    b.random_haar(2024)
+    base = [sum(ncopies[:k]) for k in range(len(confs))]
+    held = [k for k in range(len(confs)) if mine[k]]
+    b = gfx.Batch([confs[k][0] for k in held], [len(mine[k]) for k in held],
+                  precision=gfx.PREC_MIXED)
+
+    def starts():
+        for bi, k in enumerate(held):
+            for j, copy in enumerate(mine[k]):
+                b.random_haar_copy(bi, j, 2024 + base[k] + copy)
+
+    for bi, k in enumerate(held):
+        b.set_links(bi, links[k])
+    starts()
     b.overrelax(**kw)  # warm-up (graph instantiation)
-    b.random_haar(2024)
+    starts()
     res, ms_b = b.overrelax(**kw)
-    best = [b.best(k) for k in range(len(confs))]
-    upd = sum(r["sweeps"] * int(np.prod(confs[r["conf"]][0])) for r in res)
+    local_best = [None] * len(confs)
+    for bi, k in enumerate(held):
+        j, f = b.best(bi)
+        if j >= 0:
+            local_best[k] = (f, mine[k][j])
+    upd = sum(r["sweeps"] * int(np.prod(confs[held[r["conf"]]][0])) for r in res)
     b.close()
-    ms_s, base, upd_s = 0.0, 0, 0
-    for k, (d, _) in enumerate(confs):
+    ms_s, upd_s = 0.0, 0
+    for k in held:
+        d = confs[k][0]
         c = gfx.Context(d, precision=gfx.PREC_MIXED)
         c.set_links(links[k])
-        c.random_trafo_haar(2024 + base)
+        c.random_trafo_haar(2024 + base[k] + mine[k][0])
         c.overrelax(**kw)  # warm-up
-        for j in range(ncopies[k]):
-            c.random_trafo_haar(2024 + base + j)
+        for copy in mine[k]:
+            c.random_trafo_haar(2024 + base[k] + copy)
             r = c.overrelax(**kw)
             ms_s += r.ms
             upd_s += r.sweeps * int(np.prod(d))
-        base += ncopies[k]
         c.close()
+    best = gather_best(dist, ws, local_best)
+    ms_b, ms_s = max_over_ranks(dist, ms_b), max_over_ranks(dist, ms_s)
+    upd, upd_s = sum_over_ranks(dist, upd), sum_over_ranks(dist, upd_s)
+    conv = sum_over_ranks(dist, sum(r["converged"] for r in res))
     return {"workload": "%d x 16^4 (beta 6.0) + %d x 24^4 (beta 6.2) Gribov copies, Haar starts, "
                         "theta<%g" % (ncopies[0], ncopies[1], args.eps),
             "polish": POLISH_NAMES[kw["polish"]],
-            "converged": sum(r["converged"] for r in res), "copies": len(res),
+            "replicas": ws, "converged": int(conv), "copies": int(sum(ncopies)),
             "batched_s": ms_b / 1000.0, "sequential_s": ms_s / 1000.0,
             "batched_site_updates_per_s": upd / (ms_b / 1000.0),
             "sequential_site_updates_per_s": upd_s / (ms_s / 1000.0),
             "throughput_ratio": (upd / (ms_b / 1000.0)) / (upd_s / (ms_s / 1000.0)),
-            "best_copy": [{"copy": k, "F": f} for k, f in best]}
+            "best_copy": [{"copy": fc[1], "F": fc[0]} if fc else None for fc in best]}
 
 
 def run_kernels(args, dims):
@@ -333,47 +383,88 @@ def replica_inputs(rank):
     return {"mt_seed": 42 + rank, "trafo_seed": 351 + rank}
 
 
-def cpu_reference_rate(dims, sweeps, omega, seed=351):
-    """CPU port of the reference's OR update, all host threads, `sweeps` sweeps."""
+def cpu_reference_rate(dims, links, g0, sweeps, omega):
+    """The oracle's C port of the reference's OR update (overrelax.cu:149-446), built
+    for speed (-O3, FMA contraction allowed), OpenMP over one parity on all host
+    threads: `sweeps` sweeps of the given links from the start g0.  Returns site
+    updates per second, the seconds and the thread count."""
     import oracle as orc
-    o = orc.Oracle()
+    o = orc.Oracle(fast=True)
     lat = o.lattice(dims)
     V = int(np.prod(dims))
-    rng = np.random.default_rng(seed)
-    # near-identity links and the reference's random gauge start
-    z = rng.normal(size=(4 * V, 12)) * 0.3
-    gf = np.zeros((4 * V, 12))
-    gf[:, 0] = 1.0
-    gf[:, 8] = 1.0
-    gf += z
-    # rows 0,1 orthonormalized (row 2 is reconstructed by the update)
-    r0 = gf[:, 0:6:2] + 1j * gf[:, 1:6:2]
-    r1 = gf[:, 6:12:2] + 1j * gf[:, 7:12:2]
-    r0 /= np.linalg.norm(r0, axis=1, keepdims=True)
-    r1 = r1 - np.sum(r1 * np.conj(r0), axis=1, keepdims=True) * r0
-    r1 /= np.linalg.norm(r1, axis=1, keepdims=True)
-    gf[:, 0:6:2], gf[:, 1:6:2], gf[:, 6:12:2], gf[:, 7:12:2] = r0.real, r0.imag, r1.real, r1.imag
-    pm = o.pm_new(seed)
-    g = np.ascontiguousarray(o.random_init(pm, V)[:, :12])
-    o.or_halfsweep(lat, gf, g, 0, omega)  # warm the threads
+    gf12 = o.to2v(links)
+    g = np.ascontiguousarray(np.asarray(g0).reshape(-1, 18)[:, :12])
+    o.or_halfsweep(lat, gf12, g, 0, omega)  # warm the threads
     t0 = time.perf_counter()
-    o.or_sweeps(lat, gf, g, sweeps, omega)
+    o.or_sweeps(lat, gf12, g, sweeps, omega)
     dt = time.perf_counter() - t0
     return sweeps * V / dt, dt, os.cpu_count()
 
 
+CPU_SWEEPS = 10  # per sample: a bounded share of the solve's ~4500 sweeps
+
+
+def _have_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except ImportError:
+        return False
+
+
+def bench_inputs(gfx, dims, beta, therm, mt_seed, trafo_seed):
+    """The solve's inputs: Kennedy-Pendleton heatbath links (cold start, `therm`
+    sweeps, on the GPU) and the reference's random gauge start."""
+    V = int(np.prod(dims))
+    ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    ctx.set_links(gfx.unit_init(4 * V))
+    dat = mt_params_path()
+    if dat:
+        ctx.mt_load_file(dat)
+    else:
+        ctx.mt_load_params(synthetic_mt_params())
+    ctx.mt_seed(mt_seed)
+    ctx.mt_init(2 * V, 8 * V)
+    t0 = time.perf_counter()
+    ctx.thermalize(beta, therm, variant=gfx.HB_KENNEDY_PENDLETON)
+    ctx.synchronize()
+    therm_s = time.perf_counter() - t0
+    plaq = ctx.plaquette()
+    links = ctx.get_links()
+    g0 = gfx.random_init_reference(trafo_seed, V)
+    return ctx, links, g0, plaq, therm_s, dat
+
+
 # ---------------------------------------------------------------------------
 def run_reference(args, dims):
+    """The reference arm: the CPU port of the reference's OR update on the bench's own
+    inputs (the heatbath links and random start, made on the GPU before any timing),
+    all host threads, CPU_SWEEPS sweeps per step."""
     rank, ws, local, dist = dist_init(args)
     if rank != 0:
         return
+    from cudagfx_gb300 import build as b
+    b.build()
+    import cudagfx_gb300 as gfx
+    seeds = replica_inputs(rank)
     V = int(np.prod(dims))
-    sweeps = args.cpu_sweeps or 2
+    if _have_gpu():
+        ctx, links, g0, plaq, _, _ = bench_inputs(gfx, dims, args.beta, args.therm,
+                                                  seeds["mt_seed"], seeds["trafo_seed"])
+        ctx.close()
+        link_kind = "the bench's beta=%g heatbath links" % args.beta
+    else:
+        # no GPU to make the heatbath links (a CPU-only check of this arm): Haar-random
+        # links; the update's cost does not depend on the values
+        links, plaq = gfx.random_init_haar(11, 4 * V), None
+        g0 = gfx.random_init_reference(seeds["trafo_seed"], V)
+        link_kind = "Haar-random links (no GPU for the heatbath)"
+    sweeps = args.cpu_sweeps or CPU_SWEEPS
     for _ in range(max(0, min(args.warmup, 1))):
-        cpu_reference_rate(dims, 1, args.omega)
-    rates, tot = [], 0.0
+        cpu_reference_rate(dims, links, g0, 1, args.omega)
+    rates, tot, cores = [], 0.0, os.cpu_count()
     for _ in range(args.steps):
-        r, dt, cores = cpu_reference_rate(dims, sweeps, args.omega)
+        r, dt, cores = cpu_reference_rate(dims, links, g0, sweeps, args.omega)
         rates.append(r)
         tot += dt
     value = float(np.mean(rates))
@@ -382,13 +473,13 @@ def run_reference(args, dims):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "impl": "reference",
-        "config": {"workload": "%s Landau OR half-sweeps (omega=%g), CPU restatement of the "
-                               "reference update, all host threads" % ("x".join(map(str, dims)),
-                                                                       args.omega),
-                   "lattice": list(dims), "sweeps_per_step": sweeps},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": "%d OR sweeps of %s per step, OpenMP over one parity"
-                                   % (sweeps, "x".join(map(str, dims)))},
+        "config": {"workload": "%s Landau OR sweeps (omega=%g) of %s from the reference "
+                               "random start, CPU port of the reference update, all host "
+                               "threads" % ("x".join(map(str, dims)), args.omega, link_kind),
+                   "lattice": list(dims), "sweeps_per_step": sweeps, "plaquette": plaq},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "%d OR sweeps of %s per step (gcc -O3, FMA contraction), "
+                                   "OpenMP over one parity" % (sweeps, "x".join(map(str, dims)))},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -404,26 +495,15 @@ def run_gfx(args, dims):
 
     V = int(np.prod(dims))
     # ---- inputs: heatbath links (beta, cold start), reference random gauge start
-    ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
-    ctx.set_links(gfx.unit_init(4 * V))
-    dat = mt_params_path()
+    seeds = replica_inputs(rank)
+    ctx, links, g0, plaq, therm_s, dat = bench_inputs(gfx, dims, args.beta, args.therm,
+                                                      seeds["mt_seed"], seeds["trafo_seed"])
 
     def mt_source(c):
         if dat:
             c.mt_load_file(dat)
         else:
             c.mt_load_params(synthetic_mt_params())
-
-    mt_source(ctx)
-    seeds = replica_inputs(rank)
-    ctx.mt_seed(seeds["mt_seed"])
-    ctx.mt_init(2 * V, 8 * V)
-    t0 = time.perf_counter()
-    ctx.thermalize(args.beta, args.therm, variant=gfx.HB_KENNEDY_PENDLETON)
-    therm_s = time.perf_counter() - t0
-    plaq = ctx.plaquette()
-    links = ctx.get_links()
-    g0 = gfx.random_init_reference(seeds["trafo_seed"], V)
 
     def make_params(ck):
         return ctx.or_params(maxit=20000, eps=args.eps, checkinterval=ck, omega=args.omega,
@@ -528,13 +608,15 @@ def run_gfx(args, dims):
 
     cpu = None
     if rank == 0:
-        cs = args.cpu_sweeps or 2
-        rate, dt, cores = cpu_reference_rate(dims, cs, args.omega)
+        cs = args.cpu_sweeps or CPU_SWEEPS
+        rate, dt, cores = cpu_reference_rate(dims, links, g0, cs, args.omega)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": "%d OR sweeps of %s (%.1f s), CPU restatement of the reference update, "
-                         "OpenMP over one parity" % (cs, "x".join(map(str, dims)), dt)}
+               "sample": "%d OR sweeps of %s (%.1f s) on the bench's heatbath links from the "
+                         "reference start, CPU port of the reference update (gcc -O3, FMA "
+                         "contraction), OpenMP over one parity"
+                         % (cs, "x".join(map(str, dims)), dt)}
     ctx.close()
-    gribov = None if args.no_gribov else gribov_batch(args, gfx, mt_source)
+    gribov = None if args.no_gribov else gribov_batch(args, gfx, mt_source, rank, ws, dist)
     if rank != 0:
         return
     h2d = pin_links.nbytes + pin_g0.nbytes

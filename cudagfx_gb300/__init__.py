@@ -505,6 +505,7 @@ _sig("gfx_batch_set_links", _I, [_V, _I, _dp])
 _sig("gfx_batch_set_trafo", _I, [_V, _I, _I, _dp])
 _sig("gfx_batch_get_trafo", _I, [_V, _I, _I, _dp])
 _sig("gfx_batch_random_haar", _I, [_V, _c.c_uint64])
+_sig("gfx_batch_random_haar_copy", _I, [_V, _I, _I, _c.c_uint64])
 _sig("gfx_batch_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(CopyResult), _dp])
 _sig("gfx_batch_best", _I, [_V, _c.POINTER(CopyResult), _I, _c.POINTER(_I), _dp])
 _sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])
@@ -558,6 +559,9 @@ class Batch:
 
     def random_haar(self, seed):
         self._check(lib.gfx_batch_random_haar(self._h, seed))
+
+    def random_haar_copy(self, conf, copy, seed):
+        self._check(lib.gfx_batch_random_haar_copy(self._h, conf, copy, seed))
 
     def overrelax(self, params=None, **kw):
         p = params if params is not None else Context.or_params(**kw)

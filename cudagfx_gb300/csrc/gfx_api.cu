@@ -740,9 +740,9 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   s = ensure_hist(ctx, hist_need);
   if (s) return s;
 
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  EventPair ev;
+  CK(ev.create());
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   CK(cudaEventRecord(e0, ctx->stream));
 
   LoopState& H = *ctx->loop_host;
@@ -880,8 +880,6 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   CK(cudaEventSynchronize(e1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
 
   const int nrec = std::min(H.nhist, H.hist_cap);
   ctx->last_hist.resize(nrec);
@@ -1256,18 +1254,16 @@ gfx_status gfx_time_sweeps(gfx_ctx* ctx, int nsweeps, double omega, int gauge, i
   cudaError_t ge = cudaGraphInstantiate(&exec, graph, 0);
   cudaGraphDestroy(graph);
   CK(ge);
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
-  CK(cudaEventRecord(e0, ctx->stream));
-  CK(cudaGraphLaunch(exec, ctx->stream));
-  CK(cudaEventRecord(e1, ctx->stream));
-  CK(cudaEventSynchronize(e1));
+  EventPair ev;
+  cudaError_t err = ev.create();
+  if (err == cudaSuccess) err = cudaEventRecord(ev.e0, ctx->stream);
+  if (err == cudaSuccess) err = cudaGraphLaunch(exec, ctx->stream);
+  if (err == cudaSuccess) err = cudaEventRecord(ev.e1, ctx->stream);
+  if (err == cudaSuccess) err = cudaEventSynchronize(ev.e1);
   float t = 0.f;
-  CK(cudaEventElapsedTime(&t, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (err == cudaSuccess) err = cudaEventElapsedTime(&t, ev.e0, ev.e1);
   cudaGraphExecDestroy(exec);
+  CK(err);
   *ms = t;
   return GFX_OK;
 }

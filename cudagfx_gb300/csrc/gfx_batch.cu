@@ -654,6 +654,16 @@ gfx_status gfx_batch_random_haar(gfx_batch* b, uint64_t seed) {
   return GFX_OK;
 }
 
+gfx_status gfx_batch_random_haar_copy(gfx_batch* b, int conf, int copy, uint64_t seed) {
+  gfx_status s = copy_index(b, conf, copy);
+  if (s) return s;
+  const BConf& C = b->desc.c[conf];
+  launch_haar_g(C.L, (double2*)C.G64 + (size_t)copy * C.gstride64, seed, b->stream);
+  BCK(cudaGetLastError());
+  BCK(cudaStreamSynchronize(b->stream));
+  return GFX_OK;
+}
+
 gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_result* res,
                                double* ms_out) {
   if (!b || !pin) return bfail(b, GFX_ERR_ARG, "gfx_batch_overrelax: NULL argument");
@@ -679,9 +689,9 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
   }
   gfx_status s = write_states(b);
   if (s) return s;
-  cudaEvent_t e0, e1;
-  BCK(cudaEventCreate(&e0));
-  BCK(cudaEventCreate(&e1));
+  EventPair ev;
+  BCK(ev.create());
+  cudaEvent_t e0 = ev.e0, e1 = ev.e1;
   BCK(cudaEventRecord(e0, b->stream));
   // FP32 sweeps start from the FP32 copy of g (g_64_to_32 per copy)
   if (prec0 == 0) convert_batch_kernel<<<cgrid, 128, 0, b->stream>>>(b->desc, 0, -1);
@@ -774,8 +784,6 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
   BCK(cudaEventSynchronize(e1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (ms_out) *ms_out = ms;
   int all = 1;
   for (int c = 0; c < b->nconf; c++) {

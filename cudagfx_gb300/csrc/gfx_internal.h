@@ -12,6 +12,22 @@ namespace gfx {
 // Host construction of the lattice descriptor.
 Lattice make_lattice(int lx, int ly, int lz, int lt);
 
+// A start/stop pair of CUDA events that is destroyed on every exit path.
+struct EventPair {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  EventPair() = default;
+  EventPair(const EventPair&) = delete;
+  EventPair& operator=(const EventPair&) = delete;
+  cudaError_t create() {
+    cudaError_t e = cudaEventCreate(&e0);
+    return e != cudaSuccess ? e : cudaEventCreate(&e1);
+  }
+  ~EventPair() {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+};
+
 // Per-check record kept on the device (one per functional evaluation).
 struct CheckRecord {
   int iter;

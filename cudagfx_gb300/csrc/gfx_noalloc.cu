@@ -11,9 +11,11 @@
 //     is reduced by at most kBlocksPerSlice (16) blocks that stride over the slice,
 //     so the array holds 2 * 1024 * 16 partial triples and 1024 slice triples
 //     (about 0.8 MB, held on every device that loads the library until exit);
-//   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call before
-//     any stream capture;
+//   * the first call in a CUDA context looks up the array's device address with
+//     cudaGetSymbolAddress (with that context current) and keeps it for that context;
+//     make that first call before any stream capture.  A new context on the device
+//     (after cudaDeviceReset, or another context made current) is recognised by its
+//     context id and gets a fresh lookup, so a stale address is never used;
 //   * every call on a device shares the array and leaves the last call's contents
 //     in it.  Each call writes every slot it later reads, so nothing has to be
 //     cleared between calls, but calls whose kernels overlap on the GPU (different
@@ -38,7 +40,37 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// per device: the scratch array's address and the id of the context it belongs to
 double* g_scratch_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
+
+// The id of the current CUDA context (cuCtxGetId, unique for the process lifetime),
+// through the runtime's driver entry points so that the library needs no -lcuda.
+// Returns 0 when it cannot be had; the caller then looks the symbol up every call.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    looked_up = true;
+    cudaDriverEntryPointQueryResult q;
+    void* f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = (CtxGetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = (CtxGetIdFn)f;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0)
+    return 0;
+  return id;
+}
 
 // Same per-site quantities as the measurement kernel: X(x) = g(x) w(x),
 // F contribution Re tr X, tr[Delta Delta^+] = sum |AH(X)_ij|^2; each block strides
@@ -133,18 +165,30 @@ extern "C" gfx_status gfx_functional_noalloc(const void* links_device, const voi
     return GFX_ERR_ARG;
   }
   if (link_reals != 12 && link_reals != 18) return GFX_ERR_ARG;
+  if (gauge != GFX_GAUGE_LANDAU && gauge != GFX_GAUGE_COULOMB) return GFX_ERR_ARG;
+  // an error left by the caller's earlier work is not this call's: report that one is
+  // pending without clearing it (the caller still reads it with cudaGetLastError)
+  if (cudaPeekAtLastError() != cudaSuccess) {
+    std::fprintf(stderr, "gfx_functional_noalloc: an earlier CUDA error is pending: %s\n",
+                 cudaGetErrorString(cudaPeekAtLastError()));
+    return GFX_ERR_STATE;
+  }
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GFX_ERR_CUDA;
   double* scratch;
   {
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch_ptr[dev]) {
+    const unsigned long long ctx_id = current_context_id();
+    if (!g_scratch_ptr[dev] || ctx_id == 0 || ctx_id != g_scratch_ctx[dev]) {
       void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-        cudaGetLastError();
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        if (e != cudaSuccess) cudaGetLastError();  // this call's own failure
+        g_scratch_ptr[dev] = nullptr;
         return GFX_ERR_CUDA;
       }
       g_scratch_ptr[dev] = (double*)p;
+      g_scratch_ctx[dev] = ctx_id;
     }
     scratch = g_scratch_ptr[dev];
   }
@@ -164,6 +208,7 @@ extern "C" gfx_status gfx_functional_noalloc(const void* links_device, const voi
     if (ndir == 4) measure_strided_kernel<12, 4><<<grid, kBlock, 0, s>>>(L, U, G, partials);
     else measure_strided_kernel<12, 3><<<grid, kBlock, 0, s>>>(L, U, G, partials);
   }
+  if (cudaGetLastError() != cudaSuccess) return GFX_ERR_CUDA;
   // per-slice then global sums into the caller's result (gfx_functional_t layout)
   launch_reduce(L, ndir, partials, nbx, slice_sums, (Reduced*)result_device, nullptr, nullptr, 0,
                 0, 0, s);

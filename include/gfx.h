@@ -237,9 +237,13 @@ gfx_status gfx_apply_trafo(gfx_ctx *ctx);
  * process exits) with room for lt <= 1024 time slices; larger lt returns GFX_ERR_ARG.
  * links_device: FP64 links in the library's even/odd layout (link_reals 12 or 18
  * doubles per link, as a context stores them); trafo_device: FP64 12-real g in the
- * same layout; stream: a cudaStream_t or NULL.  The first call on a device looks up
- * the scratch array's address (make it before any stream capture).  All calls on a
- * device share the array; calls that overlap on the GPU race.  Asynchronous on stream. */
+ * same layout; stream: a cudaStream_t or NULL.  The first call in a CUDA context looks
+ * up the scratch array's address (make it before any stream capture); a new context on
+ * the device (e.g. after cudaDeviceReset) is detected and gets a new lookup.  gauge must
+ * be GFX_GAUGE_LANDAU or GFX_GAUGE_COULOMB (else GFX_ERR_ARG).  If a CUDA error from
+ * earlier work is pending, the call returns GFX_ERR_STATE and leaves that error for the
+ * caller.  All calls on a device share the array; calls that overlap on the GPU race.
+ * Asynchronous on stream. */
 gfx_status gfx_functional_noalloc(const void *links_device, const void *trafo_device, int lx,
                                   int ly, int lz, int lt, int link_reals, int gauge,
                                   double *result_device, void *stream);
@@ -311,6 +315,9 @@ gfx_status gfx_batch_get_trafo(gfx_batch *b, int conf, int copy, double *su3_tra
 /* Haar-random start for every copy: copy k of configuration c (global index
  * copy_base(c) + k) uses seed + global index (same generator as gfx_random_trafo_haar) */
 gfx_status gfx_batch_random_haar(gfx_batch *b, uint64_t seed);
+/* Haar-random start of one copy from its own seed (a replica that holds a share of a
+ * larger set of copies seeds each copy by its index in the whole set) */
+gfx_status gfx_batch_random_haar_copy(gfx_batch *b, int conf, int copy, uint64_t seed);
 /* fix every copy (one device loop for the whole batch); results[gfx_batch_copies()].
  * Every copy follows exactly the trajectory of gfx_overrelax on a single context with
  * the same parameters, except that the batch uses checkinterval throughout

@@ -44,10 +44,14 @@ def _p(a, t=c.c_double):
 
 
 class Oracle:
-    """CPU restatement of the reference's hot path on 12-real ('2v') fields."""
+    """CPU restatement of the reference's hot path on 12-real ('2v') fields.
 
-    def __init__(self):
-        self.lib = c.CDLL(_build.build_oracle())
+    fast=True loads the speed build of the same source (-O3, FMA contraction allowed),
+    which bench.py times as the CPU baseline; its results differ from the checker's in
+    the last bits, so tests use the default build."""
+
+    def __init__(self, fast=False):
+        self.lib = c.CDLL(_build.build_fast() if fast else _build.build_oracle())
         L = self.lib
         L.orc_plaquette.restype = c.c_double
         L.orc_gauge_functional18.restype = c.c_double
@@ -61,6 +65,7 @@ class Oracle:
                                              _fp, c.c_double]
         L.orc_link_heatbath_halfsweep.argtypes = [c.POINTER(OrcLattice), _dp, c.c_int, c.c_int,
                                                   _fp, _fp, c.c_double]
+        L.orc_link_heatbath_halfsweep_kp.argtypes = L.orc_link_heatbath_halfsweep.argtypes
         L.orc_micro_halfsweep.argtypes = [c.POINTER(OrcLattice), _dp, _dp, c.c_int, c.c_int]
 
     # ---- lattice
@@ -122,10 +127,27 @@ class Oracle:
     def micro_halfsweep(self, lat, gf12, g12, parity, ndir=4):
         self.lib.orc_micro_halfsweep(c.byref(lat), _p(gf12), _p(g12), parity, ndir)
 
-    def link_heatbath_halfsweep(self, lat, gf12, parity, nu, gauss, unif, beta):
-        self.lib.orc_link_heatbath_halfsweep(c.byref(lat), _p(gf12), parity, nu,
-                                             _p(gauss, c.c_float), _p(unif, c.c_float),
-                                             beta / 3.0)
+    def link_heatbath_halfsweep(self, lat, gf12, parity, nu, gauss, unif, beta, variant=0):
+        """variant 0: the reference's update; 1: Kennedy-Pendleton (Wilson action)"""
+        f = self.lib.orc_link_heatbath_halfsweep_kp if variant else \
+            self.lib.orc_link_heatbath_halfsweep
+        f(c.byref(lat), _p(gf12), parity, nu, _p(gauss, c.c_float), _p(unif, c.c_float),
+          beta / 3.0)
+
+    def thermalize(self, lat, gf12, m, fields, nper_g, nper_u, beta, nsweep, variant=1):
+        """nsweep sweeps of the link heatbath in the order of gfx_thermalize (nu = 0..3,
+        parity 0, 1, a twister update after each half-sweep).  m is a twister bank and
+        fields its current (gauss, unif) pair, from mt_init_fields.  Returns the
+        plaquette after each sweep and the last fields."""
+        plaq = []
+        gauss, unif = fields
+        for _ in range(nsweep):
+            for nu in range(4):
+                for par in range(2):
+                    self.link_heatbath_halfsweep(lat, gf12, par, nu, gauss, unif, beta, variant)
+                    gauss, unif = self.mt_update_fields(m, nper_g, nper_u)
+            plaq.append(self.plaquette(lat, gf12))
+        return np.array(plaq), (gauss, unif)
 
     # ---- twister bank
     def mt_new(self, params, seeds=None):

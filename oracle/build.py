@@ -1,13 +1,20 @@
 """Build recipe for the oracle (test infrastructure only).
 
   oracle/liboracle.so        the CPU restatement in gfx_oracle.c (gcc, -ffp-contract=off)
-  oracle/_ref/libref_host.so the reference's own host C files -- su3manip.c,
-                             observables.c, rngs.c, complex.c -- compiled where they
-                             lie in the reference checkout (only when it is present),
-                             plus ref_globals.c which defines the globals the
-                             reference's main would define.
-  oracle/_ref/MersenneTwister.dat   the reference's twister-parameter file, copied
-                             next to the reference build so that tests can load it.
+  oracle/liboracle_fast.so   the same restatement built for speed (-O3, FMA contraction
+                             allowed): the timed CPU baseline, not a checker
+  oracle/_ref/host_src/      unchanged copies of the reference's host C files and
+                             headers, made by copy_reference() from a reference
+                             checkout (its path is an argument or GFX_REFERENCE_DIR).
+                             The copies travel with the repository's working tree, so
+                             the builds below also run where no checkout exists.
+  oracle/_ref/libref_host.so the reference's su3manip.c, observables.c, rngs.c and
+                             complex.c, plus ref_globals.c which defines the globals
+                             the reference's main would define.
+  oracle/_ref/libref_io.so   gauge_io.c, spinor_io.c, cksum.c with libgfx's LIME records.
+  oracle/_ref/ref_gaugefix   the reference's host program flow (ref_link_main.c) over
+                             its host C files, linked against libgfx.so.
+  oracle/_ref/MersenneTwister.dat   the reference's twister-parameter file.
 
 Nothing here is part of the product; only tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg use it.
@@ -21,8 +28,36 @@ REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(REF_DIR, "libref_host.so")
 REF_DAT = os.path.join(REF_DIR, "MersenneTwister.dat")
-REFERENCE = os.environ.get("GFX_REFERENCE_DIR", "/root/reference")
+FAST_LIB = os.path.join(HERE, "liboracle_fast.so")
+# unchanged copies of the reference's host files (git-ignored; made by copy_reference)
+REFERENCE = os.path.join(REF_DIR, "host_src")
 REF_SOURCES = ["su3manip.c", "observables.c", "rngs.c", "complex.c"]
+REF_HOST_FILES = ["read_input.c", "gauge_io.c", "spinor_io.c", "cksum.c", "su3manip.c",
+                  "observables.c", "rngs.c", "complex.c", "complex.h", "cudaglobal.h",
+                  "gauge_io.h", "global.h", "observables.h", "read_input.h", "rngs.h",
+                  "spinor_io.h", "su3.h", "su3manip.h", "MersenneTwister.dat"]
+
+
+def reference_checkout(path=None):
+    """The reference checkout to copy from: `path`, else $GFX_REFERENCE_DIR, else None."""
+    path = path or os.environ.get("GFX_REFERENCE_DIR")
+    if path and os.path.exists(os.path.join(path, "global.h")):
+        return path
+    return None
+
+
+def copy_reference(path=None):
+    """Copy the reference's host files, unchanged, into oracle/_ref/host_src."""
+    src = reference_checkout(path)
+    if not src:
+        return os.path.isdir(REFERENCE)
+    os.makedirs(REFERENCE, exist_ok=True)
+    for f in REF_HOST_FILES:
+        a, b = os.path.join(src, f), os.path.join(REFERENCE, f)
+        if os.path.exists(a) and _newer(b, [a]):
+            shutil.copyfile(a, b)
+            os.chmod(b, 0o644)
+    return True
 
 
 def _run(cmd):
@@ -44,6 +79,17 @@ def build_oracle():
         _run(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-shared", "-fPIC", "-std=c99",
               src, "-o", ORACLE_LIB, "-lm"])
     return ORACLE_LIB
+
+
+def build_fast():
+    """The CPU baseline build of the restatement: -O3 with FMA contraction allowed
+    (portable flags: the same command on x86-64 and aarch64).  Its results differ from
+    the oracle's in the last bits, so it is only timed, never used as the checker."""
+    src = os.path.join(HERE, "gfx_oracle.c")
+    if _newer(FAST_LIB, [src, os.path.join(HERE, "gfx_oracle.h"), __file__]):
+        _run(["gcc", "-O3", "-ffp-contract=fast", "-fopenmp", "-shared", "-fPIC", "-std=c99",
+              src, "-o", FAST_LIB, "-lm"])
+    return FAST_LIB
 
 
 def reference_present():
@@ -115,8 +161,13 @@ def build_reference_link():
     return REF_PROGRAM
 
 
-def build():
+def build(reference=None):
+    """Build the oracle and its baseline copy; with a reference checkout (argument or
+    $GFX_REFERENCE_DIR) refresh the copies of its host files first; build the
+    reference's host libraries from the copies when they exist."""
     build_oracle()
+    build_fast()
+    copy_reference(reference)
     build_reference_host()
     build_reference_io()
 

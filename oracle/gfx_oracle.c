@@ -608,6 +608,66 @@ void orc_link_heatbath_halfsweep(const orc_lattice *L, double *gf12, int parity,
   }
 }
 
+/* Kennedy-Pendleton SU(2) heatbath for the Wilson action (A. D. Kennedy and
+ * B. J. Pendleton, Phys. Lett. B 156 (1985) 393).  The subgroup weight is
+ * exp(beta3 alpha.w), so with k = |w| the component a0 along w/k has density
+ * sqrt(1 - a0^2) exp(beta3 k a0).  One trial: 2 lambda^2 = (E + g^2 / 2) / (beta3 k)
+ * with E = -ln(1 - u0) exponential and g standard normal, a0 = 1 - 2 lambda^2,
+ * accepted when u1^2 <= 1 - lambda^2; the direction of (a1, a2, a3) is uniform on the
+ * sphere (cos theta = 2 u2 - 1, phi = 2 pi u3).  A rejected trial leaves the
+ * subgroup unchanged (alpha = 1).  alpha = a v with v = w / k (quaternion product). */
+static void heatbath_su2_kp(double al[4], const double w[4], double beta3, const float *gauss,
+                            const float *unif, long ind) {
+  double k = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2] + w[3] * w[3]);
+  al[0] = 1.0;
+  al[1] = al[2] = al[3] = 0.0;
+  if (!(k > 0.0)) return;
+  double g = (double)gauss[ind];
+  double E = -log(1.0 - (double)unif[4 * ind]);
+  double y = (E + 0.5 * g * g) / (beta3 * k); /* 2 lambda^2 */
+  double u1 = (double)unif[4 * ind + 1];
+  if (!(u1 * u1 <= 1.0 - 0.5 * y)) return;
+  double a[4], v[4];
+  for (int i = 0; i < 4; i++) v[i] = w[i] / k;
+  a[0] = 1.0 - y;
+  double norm = sqrt(fmax(0.0, 1.0 - a[0] * a[0]));
+  double cos_theta = 2.0 * (double)unif[4 * ind + 2] - 1.0;
+  double sin_theta = sqrt(fmax(0.0, 1.0 - cos_theta * cos_theta));
+  double phi = 6.2831853071795862 * (double)unif[4 * ind + 3];
+  a[1] = norm * sin_theta * cos(phi);
+  a[2] = norm * sin_theta * sin(phi);
+  a[3] = norm * cos_theta;
+  al[0] = a[0] * v[0] - a[1] * v[1] - a[2] * v[2] - a[3] * v[3];
+  al[1] = a[0] * v[1] + a[1] * v[0] - a[2] * v[3] + a[3] * v[2];
+  al[2] = a[0] * v[2] + a[2] * v[0] - a[3] * v[1] + a[1] * v[3];
+  al[3] = a[0] * v[3] + a[3] * v[0] - a[1] * v[2] + a[2] * v[1];
+}
+
+/* Cabibbo-Marinari link heatbath with the Kennedy-Pendleton SU(2) step (the Wilson
+ * action heatbath; the reference's variant above is not, see orc_link_heatbath_halfsweep).
+ * Subgroup s of link (e, nu) takes random slot 4 e + ((nu + s) & 3), so the three
+ * subgroups use independent numbers from the same fields. */
+void orc_link_heatbath_halfsweep_kp(const orc_lattice *L, double *gf12, int parity, int nu,
+                                    const float *gauss, const float *unif, double beta3) {
+  const int *tab = eo_table(L, parity);
+  long nh = L->vol / 2;
+#pragma omp parallel for schedule(static)
+  for (long e = 0; e < nh; e++) {
+    long pos = tab[e];
+    m3 st, help;
+    load12(gf12, 4 * pos + nu, help);
+    link_staple(L, gf12, pos, nu, st);
+    for (int sg = 0; sg < 3; sg++) {
+      double w[4], al[4];
+      su2_extract(help, st, SUB_A[sg], SUB_B[sg], w);
+      heatbath_su2_kp(al, w, beta3, gauss, unif, 4 * e + ((nu + sg) & 3));
+      su2_rotate(help, SUB_A[sg], SUB_B[sg], al);
+    }
+    m_normalize(help);
+    store12(gf12, 4 * pos + nu, help);
+  }
+}
+
 /* ------------------------------------------------------------------ */
 /* Mersenne Twister MT607 bank                                          */
 /* ------------------------------------------------------------------ */

@@ -74,6 +74,11 @@ void orc_micro_halfsweep(const orc_lattice *L, const double *gf12, double *g12, 
 void orc_link_heatbath_halfsweep(const orc_lattice *L, double *gf12, int parity, int nu,
                                  const float *gauss, const float *unif, double beta3);
 
+/* the same half-sweep with the Kennedy-Pendleton SU(2) step (the Wilson-action
+ * heatbath); subgroup s of link (e, nu) uses random slot 4 e + ((nu + s) & 3) */
+void orc_link_heatbath_halfsweep_kp(const orc_lattice *L, double *gf12, int parity, int nu,
+                                    const float *gauss, const float *unif, double beta3);
+
 /* Mersenne Twister MT607 bank (MersenneTwister.cu:142-229, 236-323) */
 #define ORC_MT_COUNT 4096
 #define ORC_MT_NN 19

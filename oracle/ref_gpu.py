@@ -2,10 +2,10 @@
 
 Test infrastructure only.  Two steps:
 
-prepare()  (needs the reference checkout) copies the reference's CUDA translation unit
-           (cudagaugefix.cu and the .cu/.h files it includes) and the host C files it
-           links into oracle/_ref/gpu_src/ (git-ignored) and applies the compatibility
-           shim the current toolkit needs:
+prepare(path)  (needs the reference checkout: `path` or $GFX_REFERENCE_DIR) copies the
+           reference's CUDA translation unit (cudagaugefix.cu and the .cu/.h files it
+           includes) and the host C files it links into oracle/_ref/gpu_src/
+           (git-ignored) and applies the compatibility shim the current toolkit needs:
              - the texture-reference declarations, fetch helpers and bind functions
                (dev_su3.cu:4-12, 208-218, 1644-1693) are blanked: CUDA 12+ removed
                texture references, and the reference's texture path is compiled out
@@ -14,7 +14,11 @@ prepare()  (needs the reference checkout) copies the reference's CUDA translatio
                of its name (simulated_annealing.cu:298, heatbath_thermalization.cu:561);
              - cudaThreadSynchronize -> cudaDeviceSynchronize (a -D flag);
              - empty cublas.h (included, never used) and a lime.h with the reader/writer
-               types only (the ILDG I/O is not linked).
+               types only (the ILDG I/O is not linked);
+             - the overrelaxation parameter, a literal 1.68 at overrelax.cu:416, reads
+               the __constant__ ref_omega that ref_gpu_driver.cu defines with the same
+               default 1.68 (ref_set_omega changes it), so workloads quoted at another
+               omega run through the reference's own kernel.
 build()    (needs nvcc; runs where the copied sources are, e.g. the GPU machine)
            compiles oracle/ref_gpu_driver.cu -- which includes the shimmed
            cudagaugefix.cu -- with the reference's floating-point flags into
@@ -28,7 +32,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 SRC = os.path.join(REF_DIR, "gpu_src")
 LIB = os.path.join(REF_DIR, "libref_gpu.so")
-REFERENCE = os.environ.get("GFX_REFERENCE_DIR", "/root/reference")
 
 CUDA_FILES = ["cudagaugefix.cu", "dev_su3.cu", "dev_su3.h", "overrelax.cu", "MersenneTwister.cu",
               "MersenneTwister.h", "simulated_annealing.cu", "heatbath_thermalization.cu",
@@ -41,11 +44,14 @@ BLANK = [("dev_su3.cu", 4, 12, "texture<int4,1> gf_tex"),
          ("dev_su3.cu", 1644, 1693, "bind_texture_gf")]
 REPLACE = [("simulated_annealing.cu", 'cudaMemcpyToSymbol("sa_beta"', "cudaMemcpyToSymbol(sa_beta"),
            ("heatbath_thermalization.cu", 'cudaMemcpyToSymbol("therm_beta"',
-            "cudaMemcpyToSymbol(therm_beta")]
+            "cudaMemcpyToSymbol(therm_beta"),
+           ("overrelax.cu", "overrelax(&(trafosmem[ix]), &(help), 1.68, 3);",
+            "overrelax(&(trafosmem[ix]), &(help), ref_omega, 3);")]
 
 
-def prepare():
-    if not os.path.exists(os.path.join(REFERENCE, "cudagaugefix.cu")):
+def prepare(path=None):
+    REFERENCE = path or os.environ.get("GFX_REFERENCE_DIR")
+    if not REFERENCE or not os.path.exists(os.path.join(REFERENCE, "cudagaugefix.cu")):
         return os.path.isdir(SRC)
     os.makedirs(SRC, exist_ok=True)
     for f in CUDA_FILES + HOST_C:
@@ -96,5 +102,6 @@ def build(force=False):
 
 
 if __name__ == "__main__":
-    prepare()
+    import sys
+    prepare(sys.argv[1] if len(sys.argv) > 1 else None)
     print(build(force=True))

@@ -23,6 +23,10 @@
 static unsigned int g_mtseed = 1;
 static void ref_srand_hook(unsigned int) { srand(g_mtseed); }
 
+// the overrelaxation parameter of dev_overrelax_step (a literal 1.68 in the reference,
+// overrelax.cu:416; the shim reads it from here, with the same default)
+__constant__ double ref_omega = 1.68;
+
 #define srand(x) ref_srand_hook(x)
 #define main cudagaugefix_reference_main
 #include "cudagaugefix.cu"
@@ -55,6 +59,10 @@ void ref_finalize(void) { finalize_gaugefixing(); }
 
 int ref_overrelax(int maxit, double eps, int checkinterval) {
   return overrelax_gauge(maxit, eps, checkinterval);
+}
+
+int ref_set_omega(double w) {
+  return cudaMemcpyToSymbol(ref_omega, &w, sizeof(double)) == cudaSuccess ? 0 : -1;
 }
 
 double ref_calc_functional(double* out3) {

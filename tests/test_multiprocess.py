@@ -30,7 +30,15 @@ def _rank_main(rank, ws, port, out):
     import torch
     gathered = [None] * ws
     dist.all_gather_object(gathered, seeds)
-    out[rank] = (t, gathered)
+    # Gribov copies: this rank's share, a made-up functional per copy, the best of the
+    # share, then the best over the ranks and the summed update count
+    mine = bench.split_copies([64, 32], rank, ws)
+    fake_f = lambda k, c: 2.5 + 1e-3 * ((37 * c + 11 * k) % 53)  # noqa: E731
+    local = [max(((fake_f(k, c), c) for c in mine[k]), key=lambda fc: (fc[0], -fc[1]))
+             for k in range(2)]
+    best = bench.gather_best(dist, ws, local)
+    total = bench.sum_over_ranks(dist, sum(len(m) for m in mine))
+    out[rank] = (t, gathered, mine, best, total)
     dist.destroy_process_group()
 
 
@@ -47,7 +55,15 @@ def test_two_replicas_gloo():
             p.join(120)
         assert all(p.exitcode == 0 for p in procs)
         res = dict(out)
+    fake_f = lambda k, c: 2.5 + 1e-3 * ((37 * c + 11 * k) % 53)  # noqa: E731
+    want = [max(((fake_f(k, c), c) for c in range(n)), key=lambda fc: (fc[0], -fc[1]))
+            for k, n in enumerate([64, 32])]
     for rank in range(2):
-        t, seeds = res[rank]
+        t, seeds, mine, best, total = res[rank]
         assert t == 20.0  # the slowest rank's time is every rank's
         assert seeds[0] != seeds[1]  # independent configurations
+        assert [tuple(b) for b in best] == want  # every rank holds the global best copy
+        assert total == 96
+    for k, n in enumerate([64, 32]):
+        a, b = set(res[0][2][k]), set(res[1][2][k])
+        assert not a & b and a | b == set(range(n))  # disjoint shares covering all copies

@@ -54,10 +54,18 @@ def _noalloc(gfx, U, G, dims, nreal, gauge, res):
     return f(U, G, *dims, nreal, gauge, res, None)
 
 
-@pytest.mark.parametrize("nreal", [12, 18])
-def test_functional_noalloc_matches_context_entry_point(gfx, nreal):
+# (8,6,4,10): one block per (slice, parity); (24,16,12,4): 2304 sites per
+# slice-parity, so 16 blocks stride over each slice; (2,2,2,1024): the largest time
+# extent the fixed scratch holds
+CASES = [((8, 6, 4, 10), 12, "landau"), ((8, 6, 4, 10), 18, "landau"),
+         ((24, 16, 12, 4), 12, "landau"), ((24, 16, 12, 4), 18, "coulomb"),
+         ((8, 6, 4, 10), 12, "coulomb"), ((2, 2, 2, 1024), 12, "landau")]
+
+
+@pytest.mark.parametrize("dims,nreal,gauge", CASES)
+def test_functional_noalloc_matches_context_entry_point(gfx, dims, nreal, gauge):
     torch = pytest.importorskip("torch")
-    dims = (8, 6, 4, 10)
+    gauge = gfx.COULOMB if gauge == "coulomb" else gfx.LANDAU
     vol = int(np.prod(dims))
     u = smooth_links(dims, 0.5, 41)
     res = torch.zeros(5, dtype=torch.float64, device="cuda")
@@ -66,17 +74,22 @@ def test_functional_noalloc_matches_context_entry_point(gfx, nreal):
         g = haar(vol, seed)
         G = torch.from_numpy(_pack_trafo(dims, g)).cuda()
         torch.cuda.synchronize()
-        assert _noalloc(gfx, U.data_ptr(), G.data_ptr(), dims, nreal, gfx.LANDAU,
+        assert _noalloc(gfx, U.data_ptr(), G.data_ptr(), dims, nreal, gauge,
                         res.data_ptr()) == 0
         torch.cuda.synchronize()
         got = res.cpu().numpy()
         ctx = gfx.Context(dims, link_reals=nreal)
         ctx.set_links(u)
         ctx.set_trafo(g)
-        want = ctx.functional(precision=1)
+        want = ctx.functional(gauge=gauge, precision=1)
         ctx.close()
         for k, name in enumerate(("F", "dAdA", "maxdAdA", "theta", "theta_slice_max")):
             assert got[k] == pytest.approx(getattr(want, name), rel=1e-12), (call, name)
+
+
+def test_functional_noalloc_rejects_unknown_gauge(gfx):
+    # checked with the other arguments, before any device work
+    assert _noalloc(gfx, 16, 16, (4, 4, 4, 4), 12, 7, 16) == 6  # GFX_ERR_ARG
 
 
 def test_functional_noalloc_rejects_too_many_slices(gfx):
