@@ -79,10 +79,13 @@ def parse():
                     help="skip the batched-Gribov-copies measurement")
     ap.add_argument("--gribov-copies", default="64,32",
                     help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
-    ap.add_argument("--config", choices=["c1", "c2", "c3", "c5"], default=None,
+    ap.add_argument("--gribov-paired", action="store_true",
+                    help="batched FP32 sweeps with two copies per thread (packed FP32)")
+    ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default=None,
                     help="instead of the bench: one full workload, mixed against all-FP64 "
                          "(--no-fp64 skips that solve): c1 8^4 (also on the CPU oracle), c2 "
-                         "16^3x32 SA then OR, c3 32^4 Coulomb, c5 48^3x96")
+                         "16^3x32 SA then OR, c3 32^4 Coulomb, c4 the batched Gribov copies "
+                         "alone, c5 48^3x96")
     ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2],
                     help="--kernels: OR half-sweep staging mode")
     ap.add_argument("--kernels", action="store_true",
@@ -136,7 +139,7 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
     kw = dict(maxit=20000, eps=args.eps, checkinterval=args.checkinterval or 25, omega=args.omega,
               criterion=gfx.CRIT_THETA, switch_eps=args.switch_eps,
               checkinterval_double=args.checkinterval_double,
-              polish=2 if args.polish == 2 else 0)
+              polish=2 if args.polish == 2 else 0, use_graph=0 if args.no_graph else 1)
     links = []
     for k, (d, beta) in enumerate(confs):
         V = int(np.prod(d))
@@ -160,8 +163,16 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
 
     for bi, k in enumerate(held):
         b.set_links(bi, links[k])
+    # the other FP32 sweep kernel first, for comparison: two copies per thread (packed
+    # FP32) unless --gribov-paired makes that the measured one
+    b.set_paired(0 if args.gribov_paired else 1)
     starts()
     b.overrelax(**kw)  # warm-up (graph instantiation)
+    starts()
+    _, ms_b1 = b.overrelax(**kw)
+    b.set_paired(1 if args.gribov_paired else 0)
+    starts()
+    b.overrelax(**kw)
     starts()
     res, ms_b = b.overrelax(**kw)
     local_best = [None] * len(confs)
@@ -186,13 +197,16 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
         c.close()
     best = gather_best(dist, ws, local_best)
     ms_b, ms_s = max_over_ranks(dist, ms_b), max_over_ranks(dist, ms_s)
+    ms_b1 = max_over_ranks(dist, ms_b1)
     upd, upd_s = sum_over_ranks(dist, upd), sum_over_ranks(dist, upd_s)
     conv = sum_over_ranks(dist, sum(r["converged"] for r in res))
     return {"workload": "%d x 16^4 (beta 6.0) + %d x 24^4 (beta 6.2) Gribov copies, Haar starts, "
                         "theta<%g" % (ncopies[0], ncopies[1], args.eps),
             "polish": POLISH_NAMES[kw["polish"]],
             "replicas": ws, "converged": int(conv), "copies": int(sum(ncopies)),
+            "copies_per_thread": 2 if args.gribov_paired else 1,
             "batched_s": ms_b / 1000.0, "sequential_s": ms_s / 1000.0,
+            "batched_other_kernel_s": ms_b1 / 1000.0,
             "batched_site_updates_per_s": upd / (ms_b / 1000.0),
             "sequential_site_updates_per_s": upd_s / (ms_s / 1000.0),
             "throughput_ratio": (upd / (ms_b / 1000.0)) / (upd_s / (ms_s / 1000.0)),
@@ -811,11 +825,29 @@ def run_config(args):
     print(json.dumps(out))
 
 
+def run_config_c4(args):
+    """c4  the batched Gribov copies alone (gribov_batch), one JSON line"""
+    from cudagfx_gb300 import build as b
+    b.build()
+    import cudagfx_gb300 as gfx
+    dat = mt_params_path()
+
+    def mt_source(c):
+        if dat:
+            c.mt_load_file(dat)
+        else:
+            c.mt_load_params(synthetic_mt_params())
+
+    print(json.dumps(gribov_batch(args, gfx, mt_source)))
+
+
 def main():
     args = parse()
     dims = tuple(int(x) for x in args.dims.split(","))
     if args.config in ("c1", "c2"):
         run_config_small(args)
+    elif args.config == "c4":
+        run_config_c4(args)
     elif args.config:
         run_config(args)
     elif args.kernels:

@@ -506,6 +506,7 @@ _sig("gfx_batch_set_trafo", _I, [_V, _I, _I, _dp])
 _sig("gfx_batch_get_trafo", _I, [_V, _I, _I, _dp])
 _sig("gfx_batch_random_haar", _I, [_V, _c.c_uint64])
 _sig("gfx_batch_random_haar_copy", _I, [_V, _I, _I, _c.c_uint64])
+_sig("gfx_batch_set_paired", _I, [_V, _I])
 _sig("gfx_batch_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(CopyResult), _dp])
 _sig("gfx_batch_best", _I, [_V, _c.POINTER(CopyResult), _I, _c.POINTER(_I), _dp])
 _sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])
@@ -559,6 +560,9 @@ class Batch:
 
     def random_haar(self, seed):
         self._check(lib.gfx_batch_random_haar(self._h, seed))
+
+    def set_paired(self, paired):
+        self._check(lib.gfx_batch_set_paired(self._h, 1 if paired else 0))
 
     def random_haar_copy(self, conf, copy, seed):
         self._check(lib.gfx_batch_random_haar_copy(self._h, conf, copy, seed))

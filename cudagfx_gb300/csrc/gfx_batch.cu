@@ -47,6 +47,8 @@ struct BConf {
   size_t part_base;  // first partial triple of copy 0 (copy k: + k * 2 * lt * nbx)
   int slice_base;    // first slice triple of copy 0 (copy k: + k * lt)
   int sitem_base;    // first slice-reduce item
+  int npairs;        // copy pairs (copies 2k, 2k+1; the last one alone when ncopies is odd)
+  int pitem_base;    // first paired-sweep work item
 };
 
 struct BDesc {
@@ -88,6 +90,32 @@ __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_
   V* G = (V*)(sizeof(T) == 4 ? C.G32 : C.G64) +
          (size_t)copy * (sizeof(T) == 4 ? C.gstride32 : C.gstride64);
   or_site_update<T, 12, NDIR>(C.L, s, parity, U, G, i, omega);
+}
+
+// The FP32 half-sweep with two copies per thread (or_site_update_pair: packed FP32
+// arithmetic, lane for lane the operations of or_batch_kernel<float>).  Work items are
+// (configuration, site block, copy pair), pair-minor, so the pairs of a site block run
+// side by side as in or_batch_kernel; each thread loads its 8 links once for both
+// copies.  A pair with one finished copy runs the other copy in both lanes.
+template <int NDIR>
+__global__ void __launch_bounds__(kBatchBlock, 4) or_batch_pair_kernel(BDesc d, int parity,
+                                                                       float omega) {
+  const int item = parity ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+  const int ci = conf_of(d, item, &BConf::pitem_base);
+  const BConf& C = d.c[ci];
+  const int local = item - C.pitem_base;
+  const int blk = local / C.npairs, pair = local - blk * C.npairs;
+  const int c0 = 2 * pair, c1 = min(c0 + 1, C.ncopies - 1);
+  const bool run0 = d.states[C.copy_base + c0].done == 0;
+  const bool run1 = d.states[C.copy_base + c1].done == 0;
+  if (!run0 && !run1) return;  // uniform over the block
+  const int i = blk * kBatchBlock + threadIdx.x;
+  if (i >= C.L.vh) return;
+  float4* G = (float4*)C.G32;
+  float4* Ga = G + (size_t)(run0 ? c0 : c1) * C.gstride32;
+  float4* Gb = G + (size_t)(run1 ? c1 : c0) * C.gstride32;
+  or_site_update_pair<NDIR>(C.L, site_of(C.L, i, parity), parity, (const float4*)C.U32, Ga, Gb,
+                            i, omega);
 }
 
 // The rebased FP32 polish sweep for all active copies (or_rebased_kernel per copy, the
@@ -260,7 +288,8 @@ struct gfx_batch {
   std::vector<std::array<int, 4>> dims;
   std::vector<int> copies;
   BDesc desc;
-  int nitems, nmitems, nsitems;
+  int nitems, nmitems, nsitems, npitems;
+  int paired;  // FP32 sweeps with two copies per thread (default 1)
   std::vector<void*> allocs;
   int* running;       // device
   LoopState* h_states;  // pinned
@@ -311,6 +340,11 @@ void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
         or_batch_rebased_kernel<4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
       else
         or_batch_rebased_kernel<3><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+    } else if (prec == 0 && b->paired) {
+      if (ndir == 4)
+        or_batch_pair_kernel<4><<<b->npitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
+      else
+        or_batch_pair_kernel<3><<<b->npitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
     } else if (prec == 0) {
       if (ndir == 4)
         or_batch_kernel<float, 4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
@@ -522,7 +556,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
       return s;          \
     }                    \
   } while (0)
-  int copy_base = 0, item = 0, mitem = 0, sitem = 0, slice = 0;
+  int copy_base = 0, item = 0, mitem = 0, sitem = 0, slice = 0, pitem = 0;
   size_t part = 0;
   for (int c = 0; c < nconf; c++) {
     const int* d = dims + 4 * c;
@@ -534,6 +568,8 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     C.copy_base = copy_base;
     C.nblk = (C.L.vh + kBatchBlock - 1) / kBatchBlock;
     C.item_base = item;
+    C.npairs = (C.ncopies + 1) / 2;
+    C.pitem_base = pitem;
     C.nbx = (C.L.st + kBatchBlock - 1) / kBatchBlock;
     C.mitem_base = mitem;
     C.sitem_base = sitem;
@@ -555,6 +591,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     }
     copy_base += C.ncopies;
     item += C.nblk * C.ncopies;
+    pitem += C.nblk * C.npairs;
     mitem += C.ncopies * 2 * C.L.lt * C.nbx;
     sitem += C.ncopies * C.L.lt;
     slice += C.ncopies * C.L.lt;
@@ -562,6 +599,8 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
   }
   b->ncopies = copy_base;
   b->nitems = item;
+  b->npitems = pitem;
+  b->paired = 0;
   b->nmitems = mitem;
   b->nsitems = sitem;
   b->desc.nconf = nconf;
@@ -588,6 +627,20 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
 }
 
 int gfx_batch_copies(const gfx_batch* b) { return b ? b->ncopies : 0; }
+
+gfx_status gfx_batch_set_paired(gfx_batch* b, int paired) {
+  if (!b) return bfail(nullptr, GFX_ERR_ARG, "NULL batch");
+  paired = paired ? 1 : 0;
+  if (paired == b->paired) return GFX_OK;
+  BCK(cudaStreamSynchronize(b->stream));
+  for (auto& g : b->graphs) {  // captured with the other sweep kernel
+    cudaGraphExecDestroy(g.exec);
+    cudaGraphDestroy(g.graph);
+  }
+  b->graphs.clear();
+  b->paired = paired;
+  return GFX_OK;
+}
 
 static gfx_status copy_index(gfx_batch* b, int conf, int copy) {
   if (!b || conf < 0 || conf >= b->nconf || copy < 0 || copy >= b->copies[conf])

@@ -7,6 +7,7 @@
 
 #include "gfx_device.cuh"
 #include "gfx_internal.h"
+#include "gfx_pair.cuh"
 
 namespace gfx {
 
@@ -152,38 +153,77 @@ __device__ __forceinline__ void load12_rows01(const float4* __restrict__ base, s
   m.e[1][2] = cmk(c.z, c.w);
 }
 // acc += conj(p q - r s)  and  acc += p q - r s
-__device__ __forceinline__ void acc_cross_conj(cplx<float>& acc, cplx<float> p, cplx<float> q,
-                                               cplx<float> r, cplx<float> s) {
+template <typename T>
+__device__ __forceinline__ void acc_cross_conj(cplx<T>& acc, cplx<T> p, cplx<T> q, cplx<T> r,
+                                               cplx<T> s) {
   acc.re = fm(p.re, q.re, fm(-p.im, q.im, fm(-r.re, s.re, fm(r.im, s.im, acc.re))));
   acc.im = fm(-p.re, q.im, fm(-p.im, q.re, fm(r.re, s.im, fm(r.im, s.re, acc.im))));
 }
-__device__ __forceinline__ void acc_cross(cplx<float>& acc, cplx<float> p, cplx<float> q,
-                                          cplx<float> r, cplx<float> s) {
+template <typename T>
+__device__ __forceinline__ void acc_cross(cplx<T>& acc, cplx<T> p, cplx<T> q, cplx<T> r,
+                                          cplx<T> s) {
   acc.re = fm(p.re, q.re, fm(-p.im, q.im, fm(-r.re, s.re, fm(r.im, s.im, acc.re))));
   acc.im = fm(p.re, q.im, fm(p.im, q.re, fm(-r.re, s.im, fm(-r.im, s.re, acc.im))));
 }
 
-template <int NDIR>
-__device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c, int parity,
-                                                 const float4* __restrict__ U,
-                                                 const float4* __restrict__ G,
-                                                 Mat3<float>& star) {
+// link loads of the FP32 star: scalar for one copy; for two copies in a thread (T = f2,
+// gfx_pair.cuh) the link is loaded once and broadcast to both lanes
+__device__ __forceinline__ void link_rows01(const float4* base, size_t stride, int i,
+                                            Mat3<float>& m) {
+  load12_rows01(base, stride, i, m);
+}
+__device__ __forceinline__ void link_full(const float4* base, size_t stride, int i,
+                                          Mat3<float>& m) {
+  Field<float, 12>::load(base, stride, i, m);
+}
+__device__ __forceinline__ void g_rows01(const float4* base, size_t stride, int i,
+                                         Mat3<float>& m) {
+  load12_rows01(base, stride, i, m);
+}
+__device__ __forceinline__ void g_full(const float4* base, size_t stride, int i, Mat3<float>& m) {
+  Field<float, 12>::load(base, stride, i, m);
+}
+__device__ __forceinline__ void link_rows01(const float4* base, size_t stride, int i,
+                                            Mat3<f2>& m) {
+  Mat3<float> s;
+  load12_rows01(base, stride, i, s);
+  broadcast(s, m, 2);
+}
+__device__ __forceinline__ void link_full(const float4* base, size_t stride, int i, Mat3<f2>& m) {
+  Mat3<float> s;
+  Field<float, 12>::load(base, stride, i, s);
+  broadcast(s, m, 3);
+}
+__device__ __forceinline__ void g_rows01(const GPairPtr& base, size_t stride, int i,
+                                         Mat3<f2>& m) {
+  load12_rows01(base, stride, i, m);
+}
+__device__ __forceinline__ void g_full(const GPairPtr& base, size_t stride, int i, Mat3<f2>& m) {
+  load12(base, stride, i, m);
+}
+
+// T = float with GP = const float4* (one copy), or T = f2 with GP = GPairPtr (two copies
+// of one configuration; the same operations lane for lane)
+template <typename T, typename GP, int NDIR>
+__device__ __forceinline__ void compute_star_12(const Lattice& L, const Site& c, int parity,
+                                                const float4* __restrict__ U, GP G,
+                                                Mat3<T>& star) {
   const size_t vh = (size_t)L.vh;
   const int q = 1 - parity;
-  const float4* Gq = G + (size_t)q * 3 * vh;
+  const GP Gq = G + (size_t)q * 3 * vh;
   mzero(star);
 #pragma unroll
   for (int mu = 0; mu < NDIR; mu++) {
-    Mat3<float> a, b;
-    cplx<float> P[2][3];
+    Mat3<T> a, b;
+    cplx<T> P[2][3];
     // forward: P = U g^+
-    load12_rows01(U + (size_t)(parity * 4 + mu) * 3 * vh, vh, c.i, a);
-    Field<float, 12>::load(Gq, vh, nb_fwd(L, c, mu), b);
+    link_rows01(U + (size_t)(parity * 4 + mu) * 3 * vh, vh, c.i, a);
+    g_full(Gq, vh, nb_fwd(L, c, mu), b);
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        cplx<float> x = cmulc(a.e[r][0], b.e[j][0]);
+        cplx<T> x = cmulc(a.e[r][0], b.e[j][0]);
         cmacc(x, a.e[r][1], b.e[j][1]);
         cmacc(x, a.e[r][2], b.e[j][2]);
         P[r][j] = x;
@@ -194,13 +234,13 @@ __device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c
     acc_cross_conj(star.e[2][2], P[0][0], P[1][1], P[0][1], P[1][0]);
     // backward: Q = g(x-mu) U_mu(x-mu), w += Q^+
     const int jb = nb_bwd(L, c, mu);
-    load12_rows01(Gq, vh, jb, b);
-    Field<float, 12>::load(U + (size_t)(q * 4 + mu) * 3 * vh, vh, jb, a);
+    g_rows01(Gq, vh, jb, b);
+    link_full(U + (size_t)(q * 4 + mu) * 3 * vh, vh, jb, a);
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
       for (int j = 0; j < 3; j++) {
-        cplx<float> x = cmul(b.e[r][0], a.e[0][j]);
+        cplx<T> x = cmul(b.e[r][0], a.e[0][j]);
         cmac(x, b.e[r][1], a.e[1][j]);
         cmac(x, b.e[r][2], a.e[2][j]);
         P[r][j] = x;
@@ -211,6 +251,14 @@ __device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c
     acc_cross(star.e[1][2], P[0][2], P[1][0], P[0][0], P[1][2]);
     acc_cross(star.e[2][2], P[0][0], P[1][1], P[0][1], P[1][0]);
   }
+}
+
+template <int NDIR>
+__device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c, int parity,
+                                                 const float4* __restrict__ U,
+                                                 const float4* __restrict__ G,
+                                                 Mat3<float>& star) {
+  compute_star_12<float, const float4*, NDIR>(L, c, parity, U, G, star);
 }
 
 // One overrelaxation site update (overrelax.cu:335-446) of site i of parity `parity`
@@ -239,6 +287,24 @@ __device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, 
     overrelax_rows01(gn, gold, g, omega);
   }
   Field<T, 12>::store(Gp, vh, i, gn);
+}
+
+// The FP32 update of site i for two copies of one configuration at once (T = f2):
+// lane for lane the operations of or_site_update<float, 12, NDIR>.  Ga, Gb: the two
+// copies' g fields (Ga == Gb runs one copy twice, which stores the same values twice).
+template <int NDIR>
+__device__ __forceinline__ void or_site_update_pair(const Lattice& L, const Site& c, int parity,
+                                                    const float4* __restrict__ U, float4* Ga,
+                                                    float4* Gb, int i, float omega) {
+  const size_t vh = (size_t)L.vh;
+  GPairPtr G;
+  G.a = Ga;
+  G.b = Gb;
+  Mat3<f2> star, gold, gn;
+  compute_star_12<f2, GPairPtr, NDIR>(L, c, parity, U, G, star);
+  load12(G + (size_t)parity * 3 * vh, vh, i, gold);
+  or_update_composed(gold, star, f2(omega), gn);
+  store12(Ga + (size_t)parity * 3 * vh, Gb + (size_t)parity * 3 * vh, vh, i, gn);
 }
 
 // Per-site functional from X = g w (overrelax.cu:451-605, see measure_kernel):

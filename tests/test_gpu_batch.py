@@ -55,3 +55,25 @@ def test_batch_best_copy(gfx):
     k, f = b.best(0)
     fs = [r["F"] for r in res[:6]]
     assert k == int(np.argmax(fs)) and f == max(fs)
+
+
+@pytest.mark.parametrize("ncopies", [[5, 3], [2, 7]])
+def test_paired_sweeps_bit_identical_to_one_copy_per_thread(gfx, ncopies):
+    # two copies per thread in packed FP32 arithmetic give every copy the bits of the
+    # one-copy-per-thread kernel, also when the two copies of a pair stop at different
+    # checks (the finished copy's lane then repeats its partner)
+    kw = dict(maxit=4000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA,
+              switch_eps=1e-9, checkinterval_double=5, polish=0)
+    out = []
+    for paired in (1, 0):
+        b, _ = _batch(gfx, 2, ncopies)
+        b.set_paired(paired)
+        res, _ = b.overrelax(**kw)
+        out.append((res, [b.get_trafo(c, k) for c in range(2) for k in range(ncopies[c])]))
+        b.close()
+    (rp, gp), (r1, g1) = out
+    assert [r["iterations"] for r in rp] == [r["iterations"] for r in r1]
+    assert len({r["sweeps_single"] for r in rp}) > 1  # copies leave the FP32 phase apart
+    assert [r["F"] for r in rp] == [r["F"] for r in r1]
+    for a, b in zip(gp, g1):
+        assert np.array_equal(a, b)
