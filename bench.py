@@ -565,16 +565,26 @@ def run_gfx(args, dims):
     pin_g0[...] = g0
     pin_out = gfx.pinned_empty(g0.shape)
     e2e_t, e2e_upd, e2e_dev = 0.0, 0, 0.0
+    parts = {"set_links": 0.0, "set_trafo": 0.0, "overrelax": 0.0, "get_trafo": 0.0}
     for _ in range(args.steps):
         ctx.synchronize()
         t0 = time.perf_counter()
         ctx.set_links(pin_links)
+        t1 = time.perf_counter()
         ctx.set_trafo(pin_g0)
+        t2 = time.perf_counter()
         r = ctx.overrelax(params)
+        t3 = time.perf_counter()
         ctx.get_trafo_into(pin_out)
-        e2e_t += time.perf_counter() - t0
+        t4 = time.perf_counter()
+        e2e_t += t4 - t0
         e2e_upd += r.sweeps * V
         e2e_dev += r.ms / 1000.0
+        # each call returns after its work on the device is done
+        parts["set_links"] += t1 - t0
+        parts["set_trafo"] += t2 - t1
+        parts["overrelax"] += t3 - t2
+        parts["get_trafo"] += t4 - t3
     e2e_t = max_over_ranks(dist, e2e_t)
     e2e_value = e2e_upd * ws / e2e_t
 
@@ -673,7 +683,12 @@ def run_gfx(args, dims):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": pin_out.nbytes,
                 # wall time per step, and the solve's device time within it
-                "s_per_step": e2e_t / args.steps, "solve_device_s_per_step": e2e_dev / args.steps},
+                "s_per_step": e2e_t / args.steps, "solve_device_s_per_step": e2e_dev / args.steps,
+                # wall seconds per step of each public call (host-timed; every call
+                # synchronizes before it returns); overrelax_host_s = its wall time
+                # outside the device-timed solve
+                "breakdown_s": dict({k: v / args.steps for k, v in parts.items()},
+                                    overrelax_host_s=(parts["overrelax"] - e2e_dev) / args.steps)},
         "clocks": clocks,
         "gpu_launches": int(launches),
         "gribov_batch": gribov,

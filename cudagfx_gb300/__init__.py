@@ -379,6 +379,9 @@ class Context:
         self._check(lib.gfx_time_sweeps(self._h, n, omega, gauge, precision, _ptr(ms)))
         return float(ms[0])
 
+    def set_fused_check(self, fused):
+        self._check(lib.gfx_set_fused_check(self._h, 1 if fused else 0))
+
     def launch_count(self):
         return lib.gfx_launch_count(self._h)
 
@@ -507,6 +510,7 @@ _sig("gfx_batch_get_trafo", _I, [_V, _I, _I, _dp])
 _sig("gfx_batch_random_haar", _I, [_V, _c.c_uint64])
 _sig("gfx_batch_random_haar_copy", _I, [_V, _I, _I, _c.c_uint64])
 _sig("gfx_batch_set_paired", _I, [_V, _I])
+_sig("gfx_set_fused_check", _I, [_V, _I])
 _sig("gfx_batch_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(CopyResult), _dp])
 _sig("gfx_batch_best", _I, [_V, _c.POINTER(CopyResult), _I, _c.POINTER(_I), _dp])
 _sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])

@@ -221,6 +221,21 @@ void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
   ctx->launches += 1;
 }
 
+void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n) {
+  if (prec != 0 || n < 1 || !ctx->fuse_check || !fused_check_ok(ctx->L, ctx->link_nr32)) {
+    enqueue_sweeps(ctx, prec, ndir, omega, n);
+    enqueue_measure(ctx, prec, prec, ndir);
+    return;
+  }
+  enqueue_sweeps(ctx, 0, ndir, omega, n - 1);
+  launch_or_halfsweep(0, 12, ndir, ctx->L, ctx->U32, ctx->G32, 0, omega, ctx->or_block[0],
+                      ctx->or_pf[0], ctx->stream);
+  launch_or_halfsweep_measure(ndir, ctx->L, ctx->U32, ctx->G32, omega, ctx->or_pf[0] == 2,
+                              ctx->partials, ctx->stream);
+  launch_measure_even(ndir, ctx->L, ctx->U32, ctx->G32, ctx->partials, ctx->stream);
+  ctx->launches += 3;
+}
+
 void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
                            unsigned long long handle, int use_handle) {
   const int nbx = measure_blocks_x(ctx->L, meas_block(ctx));
@@ -345,6 +360,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->block = 128;
   ctx->or_block[0] = ctx->or_block[1] = ctx->or_block[2] = 128;
   ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 2;  // odd half-sweeps in reverse order
+  ctx->fuse_check = 1;
   ctx->Udf = ctx->Gdf = nullptr;
   ctx->udf_valid = false;
   ctx->Ur = ctx->W0 = nullptr;
@@ -434,6 +450,13 @@ gfx_status gfx_set_device(int device) {
     cudaGetLastError();
     return fail(nullptr, GFX_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
   }
+  return GFX_OK;
+}
+
+gfx_status gfx_set_fused_check(gfx_ctx* ctx, int fused) {
+  if (!ctx) return fail(nullptr, GFX_ERR_ARG, "NULL context");
+  ctx->fuse_check = fused ? 1 : 0;
+  destroy_graphs(ctx);  // loop bodies captured with the other check
   return GFX_OK;
 }
 
@@ -658,8 +681,7 @@ void gfx_or_params_default(gfx_or_params* p) {
 // body of the device-side loop: ck sweeps, measurement, reduction + check
 static void enqueue_body(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
                          unsigned long long handle, int use_handle) {
-  enqueue_sweeps(ctx, prec, ndir, omega, ck);
-  enqueue_measure(ctx, prec, prec, ndir);
+  enqueue_sweeps_measure(ctx, prec, ndir, omega, ck);
   enqueue_reduce(ctx, ndir, true, ck, handle, use_handle);
 }
 
@@ -768,9 +790,8 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
 
   int sweeps_single = 0, sweeps_double = 0, sweeps_df = 0, sweeps_rb = 0;
   // iteration 0: sweep, then the first check (overrelax.cu:710-789)
-  enqueue_sweeps(ctx, prec, ndir, p.omega, 1);
+  enqueue_sweeps_measure(ctx, prec, ndir, p.omega, 1);
   (prec == 0 ? sweeps_single : sweeps_double)++;
-  enqueue_measure(ctx, prec, prec, ndir);
   enqueue_reduce(ctx, ndir, true, 0, 0, 0);
   CK(cudaGetLastError());
   s = read_loop(ctx);

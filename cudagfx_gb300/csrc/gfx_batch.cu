@@ -161,7 +161,10 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
     const int i = t * C.L.st + k;
     const Site c = site_of(C.L, i, parity);
     Mat3<TC> star, g;
-    compute_star<TC, TC, 12, TSG, 12, NDIR>(C.L, c, parity, U, G, star);
+    if constexpr (sizeof(TC) == 4 && sizeof(TSG) == 4)
+      compute_star_f32<NDIR>(C.L, c, parity, (const float4*)U, (const float4*)G, star);
+    else
+      compute_star<TC, TC, 12, TSG, 12, NDIR>(C.L, c, parity, U, G, star);
     constexpr int NCG = Field<TSG, 12>::NCHUNK;
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * C.L.vh, (size_t)C.L.vh, i, g);
     site_functional(g, star, f, dd);

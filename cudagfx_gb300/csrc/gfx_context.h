@@ -28,6 +28,7 @@ struct gfx_ctx {
   int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
   int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch, 2 plain
                     // with the odd half-sweep's blocks in reverse order (the default)
+  int fuse_check;   // FP32 checks fused into the last odd half-sweep when possible (default 1)
   double tune_sweep_ms[2], tune_measure_ms[2];
   int tune_ck;
   cudaStream_t stream;
@@ -133,6 +134,9 @@ gfx_status prepare_rebased(gfx_ctx* ctx, int ndir);
 void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega);
 void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
 void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir);
+// n sweeps followed by the check's measurement (the same partials either way; FP32
+// with fused_check_ok: the last odd half-sweep writes the odd sites' partials)
+void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
 void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
                     unsigned long long handle, int use_handle);
 // re-pack the FP64 links as nr reals per link (12 or 18)

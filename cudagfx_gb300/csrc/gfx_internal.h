@@ -73,6 +73,17 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
 void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
                     const void* G, double* partials, int block, cudaStream_t s);
 int measure_blocks_x(const Lattice& L, int block);
+// sites per measurement block (the grouping of the partial sums)
+constexpr int kMeasBlock = 128;
+// FP32 checks fused into the last odd half-sweep: possible for 12-real FP32 links when
+// every time slice holds whole measurement blocks of each parity
+bool fused_check_ok(const Lattice& L, int link_nr32);
+// the odd half-sweep that also writes the odd sites' partials (launch_measure's layout)
+void launch_or_halfsweep_measure(int ndir, const Lattice& L, const void* U, void* G, double omega,
+                                 int rev, double* partials, cudaStream_t s);
+// launch_measure's FP32 even-site blocks only
+void launch_measure_even(int ndir, const Lattice& L, const void* U, const void* G,
+                         double* partials, cudaStream_t s);
 void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
                    Reduced* out, LoopState* loop, CheckRecord* hist, int advance,
                    unsigned long long graph_handle, int use_handle, cudaStream_t s);

@@ -117,13 +117,77 @@ __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
     const int i = t * L.st + k;
     const Site c = site_of(L, i, parity);
     Mat3<TC> star, g;
-    compute_star<TC, TSU, NRU, TSG, 12, NDIR>(L, c, parity, U, G, star);
+    if constexpr (sizeof(TC) == 4 && sizeof(TSG) == 4 && NRU == 12)
+      compute_star_f32<NDIR>(L, c, parity, (const float4*)U, (const float4*)G, star);
+    else
+      compute_star<TC, TSU, NRU, TSG, 12, NDIR>(L, c, parity, U, G, star);
     constexpr int NCG = Field<TSG, 12>::NCHUNK;
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * L.vh, (size_t)L.vh, i, g);
     site_functional(g, star, f, d);
   }
   const int nbx = gridDim.x;
   block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + blockIdx.x));
+}
+
+// ---------------------------------------------------------------------------
+// The last odd half-sweep before a check, fused with the check's odd-site partials
+// (FP32, 12-real links).  The star w(x) of an odd site depends only on the links and
+// the even g, which this half-sweep does not change, so X = g_new(x) w(x) -- the
+// quantity the measurement kernel forms for that site after the sweep -- is one
+// product away from the registers of the update.  Each block of kMeasBlock sites
+// is exactly one measurement block (slice t, block bx; needs st % kMeasBlock == 0)
+// and reduces in the measurement kernel's order, so the partials, and with them
+// every check value, are bit-identical to the separate measurement; that kernel
+// then runs over the even sites only.  This removes the measurement's second read
+// of every link (each link has one even and one odd end).
+// ---------------------------------------------------------------------------
+template <int NDIR>
+__global__ void __launch_bounds__(kMeasBlock, 6) or_halfsweep_measure_kernel(
+    Lattice L, const float4* U, float4* G, float omega, int rev, int nbx, double* partials) {
+  const int blk = rev ? (int)gridDim.x - 1 - (int)blockIdx.x : (int)blockIdx.x;
+  const int i = blk * kMeasBlock + threadIdx.x;  // < vh: the grid covers vh exactly
+  const int parity = 1;
+  const size_t vh = (size_t)L.vh;
+  const Site c = site_of(L, i, parity);
+  float4* Gp = G + (size_t)parity * 3 * vh;
+  Mat3<float> star, gold, gn;
+  compute_star_f32<NDIR>(L, c, parity, U, G, star);
+  Field<float, 12>::load(Gp, vh, i, gold);
+  or_update_composed(gold, star, omega, gn);
+  Field<float, 12>::store(Gp, vh, i, gn);
+  row2_from_01(gn);  // as the measurement's load of the stored rows
+  double f, d;
+  site_functional(gn, star, f, d);
+  const int t = blk / nbx, bx = blk - t * nbx;
+  block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + bx));
+}
+
+bool fused_check_ok(const Lattice& L, int link_nr32) {
+  return link_nr32 == 12 && L.st % kMeasBlock == 0;
+}
+
+void launch_or_halfsweep_measure(int ndir, const Lattice& L, const void* U, void* G, double omega,
+                                 int rev, double* partials, cudaStream_t s) {
+  const int nbx = measure_blocks_x(L, kMeasBlock);
+  const dim3 grid(L.vh / kMeasBlock);
+  if (ndir == 4)
+    or_halfsweep_measure_kernel<4><<<grid, kMeasBlock, 0, s>>>(
+        L, (const float4*)U, (float4*)G, (float)omega, rev, nbx, partials);
+  else
+    or_halfsweep_measure_kernel<3><<<grid, kMeasBlock, 0, s>>>(
+        L, (const float4*)U, (float4*)G, (float)omega, rev, nbx, partials);
+}
+
+// the measurement's even-site blocks only (the odd ones come from the fused sweep)
+void launch_measure_even(int ndir, const Lattice& L, const void* U, const void* G,
+                         double* partials, cudaStream_t s) {
+  const dim3 grid(measure_blocks_x(L, kMeasBlock), 1, L.lt);
+  if (ndir == 4)
+    measure_kernel<float, float, 12, float, 4><<<grid, kMeasBlock, 0, s>>>(
+        L, (const float4*)U, (const float4*)G, partials);
+  else
+    measure_kernel<float, float, 12, float, 3><<<grid, kMeasBlock, 0, s>>>(
+        L, (const float4*)U, (const float4*)G, partials);
 }
 
 int measure_blocks_x(const Lattice& L, int block) { return (L.st + block - 1) / block; }

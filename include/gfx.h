@@ -248,6 +248,11 @@ gfx_status gfx_functional_noalloc(const void *links_device, const void *trafo_de
                                   int ly, int lz, int lt, int link_reals, int gauge,
                                   double *result_device, void *stream);
 
+/* FP32 convergence checks fused into the last odd half-sweep before the check (1, the
+ * default; used when the FP32 links hold 12 reals and each time slice holds whole
+ * 128-site blocks of each parity) or a separate measurement (0); the check values are
+ * bit-identical */
+gfx_status gfx_set_fused_check(gfx_ctx *ctx, int fused);
 /* device time (CUDA events on the context's stream) of nsweeps plain OR sweeps, run
  * as one CUDA graph (back to back, as in gfx_overrelax's device loop) */
 gfx_status gfx_time_sweeps(gfx_ctx *ctx, int nsweeps, double omega, int gauge, int precision,
