@@ -215,7 +215,8 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
 
 def run_kernels(args, dims):
     """A short fixed workload for profiler captures: 3 FP32 OR sweeps, an FP32 and an
-    FP64 functional, 1 FP64 OR sweep, 3 rebased FP32 sweeps and their functional, one
+    FP64 functional, 31 sweeps of the FP32 convergence loop with a check every 10 (the
+    fused check), 1 FP64 OR sweep, 3 rebased FP32 sweeps and their functional, one
     SA step with one microcanonical step, and one link-heatbath sweep in FP64 and one in
     FP32 arithmetic.  The OR sweeps use --staging (2, the tuner's
     choice on 32^4: the odd half-sweep in reverse block order)."""
@@ -229,6 +230,10 @@ def run_kernels(args, dims):
     ctx.or_sweeps(3, omega=args.omega, precision=0)
     ctx.functional(precision=0)
     ctx.functional(precision=1)
+    # a few FP32 checks of the convergence loop, host-driven so that each launch is
+    # visible to a profiler: the fused odd half-sweep and the even-site measurement
+    ctx.overrelax(maxit=31, eps=1e-30, checkinterval=10, omega=args.omega,
+                  criterion=gfx.CRIT_THETA, switch_eps=1e-40, use_graph=0)
     ctx.or_sweeps(1, omega=args.omega, precision=1)
     ctx.or_sweeps(3, omega=args.omega, precision=3)
     ctx.functional(precision=3)

@@ -156,22 +156,26 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
   const VG* G = (const VG*)(sizeof(TSG) == 4 ? C.G32 : C.G64) +
                 (size_t)copy * (sizeof(TSG) == 4 ? C.gstride32 : C.gstride64);
   const int k = bx * blockDim.x + threadIdx.x;
+  constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
   double f = 0.0, dd = 0.0;
+  float f32 = 0.0f, d32 = 0.0f;
   if (k < C.L.st) {
     const int i = t * C.L.st + k;
     const Site c = site_of(C.L, i, parity);
     Mat3<TC> star, g;
-    if constexpr (sizeof(TC) == 4 && sizeof(TSG) == 4)
+    if constexpr (F32)
       compute_star_f32<NDIR>(C.L, c, parity, (const float4*)U, (const float4*)G, star);
     else
       compute_star<TC, TC, 12, TSG, 12, NDIR>(C.L, c, parity, U, G, star);
     constexpr int NCG = Field<TSG, 12>::NCHUNK;
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * C.L.vh, (size_t)C.L.vh, i, g);
-    site_functional(g, star, f, dd);
+    if constexpr (F32) site_functional_f32(g, star, f32, d32);
+    else site_functional(g, star, f, dd);
   }
   double* out = d.partials +
                 3 * (C.part_base + (size_t)copy * per_copy + (size_t)(parity * C.L.lt + t) * C.nbx + bx);
-  block_reduce3(f, dd, dd, out);
+  if constexpr (F32) block_reduce3_f32(f32, d32, out);
+  else block_reduce3(f, dd, dd, out);
 }
 
 // the same partials from the rebased fields (measure_rebased_kernel per copy)

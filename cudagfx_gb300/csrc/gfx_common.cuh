@@ -363,6 +363,69 @@ __device__ __forceinline__ void block_reduce3(double f, double d, double m, doub
   }
 }
 
+// The FP32 checks' per-site values in FP32: GB300 runs FP64 at a small fraction of its
+// FP32 rate, and the FP64 conversions and shuffles of the general path cost a check on
+// the FP32 links about as much as a sweep.  The sums over the 32 sites of a warp are
+// FP32 (relative rounding ~3e-7, well inside what the FP32 phase's plateau test
+// resolves); every sum above the warp -- warps of a block, blocks, slices -- is FP64.
+__device__ __forceinline__ void site_functional_f32(const Mat3<float>& g, const Mat3<float>& star,
+                                                    float& f, float& d) {
+  Mat3<float> X;
+  mul(X, g, star);
+  f = X.e[0][0].re + X.e[1][1].re + X.e[2][2].re;
+  const float tim = (X.e[0][0].im + X.e[1][1].im + X.e[2][2].im) * (1.0f / 3.0f);
+  float acc = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float di = X.e[a][a].im - tim;
+    acc = fm(di, di, acc);
+  }
+  float off = 0.0f;
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = a + 1; b < 3; b++) {
+      const float re = (X.e[a][b].re - X.e[b][a].re) * 0.5f;
+      const float im = (X.e[a][b].im + X.e[b][a].im) * 0.5f;
+      off = fm(im, im, fm(re, re, off));
+    }
+  d = fm(2.0f, off, acc);
+}
+
+// block sums of the FP32 per-site values: FP32 within each warp (fixed butterfly),
+// FP64 across the warps in the order of block_reduce3; the max in FP32 (exact)
+__device__ __forceinline__ void block_reduce3_f32(float f, float d, double* out) {
+  __shared__ double sh[3][32];
+  float m = d;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    f += __shfl_xor_sync(0xffffffffu, f, o);
+    d += __shfl_xor_sync(0xffffffffu, d, o);
+    m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    sh[0][w] = (double)f;
+    sh[1][w] = (double)d;
+    sh[2][w] = (double)m;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    double fs = l < nw ? sh[0][l] : 0.0;
+    double ds = l < nw ? sh[1][l] : 0.0;
+    double ms = l < nw ? sh[2][l] : 0.0;
+    fs = warp_sum(fs);
+    ds = warp_sum(ds);
+    ms = warp_max(ms);
+    if (l == 0) {
+      out[0] = fs;
+      out[1] = ds;
+      out[2] = ms;
+    }
+  }
+}
+
 enum { CRIT_MAXDADA = 0, CRIT_THETA = 1, CRIT_THETA_SLICES = 2 };
 
 // Totals over the slices, then (when loop is given) one check of the convergence loop:

@@ -112,21 +112,26 @@ __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
   // the links and g they share are read from L2 the second time
   const int parity = blockIdx.y, t = blockIdx.z;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
   double f = 0.0, d = 0.0;
+  float f32 = 0.0f, d32 = 0.0f;
   if (k < L.st) {
     const int i = t * L.st + k;
     const Site c = site_of(L, i, parity);
     Mat3<TC> star, g;
-    if constexpr (sizeof(TC) == 4 && sizeof(TSG) == 4 && NRU == 12)
+    if constexpr (F32 && NRU == 12)
       compute_star_f32<NDIR>(L, c, parity, (const float4*)U, (const float4*)G, star);
     else
       compute_star<TC, TSU, NRU, TSG, 12, NDIR>(L, c, parity, U, G, star);
     constexpr int NCG = Field<TSG, 12>::NCHUNK;
     Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * L.vh, (size_t)L.vh, i, g);
-    site_functional(g, star, f, d);
+    if constexpr (F32) site_functional_f32(g, star, f32, d32);
+    else site_functional(g, star, f, d);
   }
   const int nbx = gridDim.x;
-  block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + blockIdx.x));
+  double* out = partials + 3 * ((size_t)(parity * L.lt + t) * nbx + blockIdx.x);
+  if constexpr (F32) block_reduce3_f32(f32, d32, out);
+  else block_reduce3(f, d, d, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -156,10 +161,10 @@ __global__ void __launch_bounds__(kMeasBlock, 6) or_halfsweep_measure_kernel(
   or_update_composed(gold, star, omega, gn);
   Field<float, 12>::store(Gp, vh, i, gn);
   row2_from_01(gn);  // as the measurement's load of the stored rows
-  double f, d;
-  site_functional(gn, star, f, d);
+  float f, d;
+  site_functional_f32(gn, star, f, d);
   const int t = blk / nbx, bx = blk - t * nbx;
-  block_reduce3(f, d, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + bx));
+  block_reduce3_f32(f, d, partials + 3 * ((size_t)(parity * L.lt + t) * nbx + bx));
 }
 
 bool fused_check_ok(const Lattice& L, int link_nr32) {

@@ -18,6 +18,10 @@ double orxeps;
 gfx_saparam_list saparam;
 gfx_thermparam_list thermparam;
 void *dev_gf, *dev_trafo1;
+// host geometry tables of the reference (global.h:104-119), filled by init_gaugefixing
+// and init_thermalization as the reference's do (cudagaugefix.cu:285-323, 72-196);
+// the reference's host observables (observables.c) walk the lattice through nn
+int *nn, *ind, *lexic2eo, *nn_eo, *nn_oe, *eoidx_even, *eoidx_odd;
 }
 
 namespace {
@@ -61,6 +65,14 @@ void create_context() {
   dev_trafo1 = (void*)g_ctx;
 }
 
+void free_tables() {
+  int** t[] = {&nn, &ind, &lexic2eo, &nn_eo, &nn_oe, &eoidx_even, &eoidx_odd};
+  for (int** p : t) {
+    std::free(*p);
+    *p = nullptr;
+  }
+}
+
 void require_ctx(const char* who) {
   if (!g_ctx) {
     std::fprintf(stderr, "%s called before init_gaugefixing/init_thermalization\n", who);
@@ -71,8 +83,61 @@ void require_ctx(const char* who) {
 
 extern "C" {
 
+// Lexicographic site pos = x + LX (y + LY (z + LZ t)).  nn[8 pos + mu] is the site
+// x + mu and nn[8 pos + 4 + mu] the site x - mu (mu = x, y, z, t; periodic); ind[pos] =
+// pos; lexic2eo[pos] numbers the sites of each parity (x + y + z + t even / odd) in
+// lexicographic order; eoidx_even / eoidx_odd map those numbers back to pos; nn_eo /
+// nn_oe hold the eo numbers of the neighbours of even / odd sites, in nn's order.
+int gfx_legacy_init_tables(void) {
+  free_tables();
+  const long v = (long)LX * LY * LZ * T;
+  if (LX < 1 || LY < 1 || LZ < 1 || T < 1 || v % 2) return -1;
+  nn = (int*)std::malloc(sizeof(int) * 8 * v);
+  ind = (int*)std::malloc(sizeof(int) * v);
+  lexic2eo = (int*)std::malloc(sizeof(int) * v);
+  nn_eo = (int*)std::malloc(sizeof(int) * 4 * v);
+  nn_oe = (int*)std::malloc(sizeof(int) * 4 * v);
+  eoidx_even = (int*)std::malloc(sizeof(int) * v / 2);
+  eoidx_odd = (int*)std::malloc(sizeof(int) * v / 2);
+  if (!nn || !ind || !lexic2eo || !nn_eo || !nn_oe || !eoidx_even || !eoidx_odd) {
+    free_tables();
+    return -1;
+  }
+  const int ext[4] = {LX, LY, LZ, T};
+  const long stride[4] = {1, LX, (long)LX * LY, (long)LX * LY * LZ};
+  long ne = 0, no = 0;
+  for (long pos = 0; pos < v; pos++) {
+    long c[4], r = pos;
+    for (int mu = 0; mu < 4; mu++) {
+      c[mu] = r % ext[mu];
+      r /= ext[mu];
+    }
+    for (int mu = 0; mu < 4; mu++) {
+      const long up = c[mu] + 1 == ext[mu] ? -(ext[mu] - 1) : 1;
+      const long dn = c[mu] == 0 ? ext[mu] - 1 : -1;
+      nn[8 * pos + mu] = (int)(pos + up * stride[mu]);
+      nn[8 * pos + 4 + mu] = (int)(pos + dn * stride[mu]);
+    }
+    ind[pos] = (int)pos;
+    if ((c[0] + c[1] + c[2] + c[3]) % 2 == 0) {
+      eoidx_even[ne] = (int)pos;
+      lexic2eo[pos] = (int)ne++;
+    } else {
+      eoidx_odd[no] = (int)pos;
+      lexic2eo[pos] = (int)no++;
+    }
+  }
+  for (long pos = 0; pos < v; pos++) {
+    int* out = ((pos % LX + (pos / LX) % LY + (pos / stride[2]) % LZ + pos / stride[3]) % 2 == 0
+                    ? nn_eo : nn_oe) + 8 * (long)lexic2eo[pos];
+    for (int j = 0; j < 8; j++) out[j] = lexic2eo[nn[8 * pos + j]];
+  }
+  return 0;
+}
+
 void init_gaugefixing(gfx_su3* gf, gfx_su3* trafo) {
   create_context();
+  if (gfx_legacy_init_tables() != 0) die(200, "Error in init_gaugefixing(): host tables");
   if (gfx_set_links(g_ctx, (const double*)gf) != GFX_OK ||
       gfx_set_trafo(g_ctx, (const double*)trafo) != GFX_OK) {
     std::printf("Error in init_gaugefixing(): %s. Aborting...\n", gfx_last_error(g_ctx));
@@ -87,10 +152,12 @@ void finalize_gaugefixing(void) {
   if (g_ctx) gfx_destroy(g_ctx);
   g_ctx = nullptr;
   dev_gf = dev_trafo1 = nullptr;
+  free_tables();
 }
 
 void init_thermalization(gfx_su3* gf) {
   create_context();
+  if (gfx_legacy_init_tables() != 0) die(200, "Error in init_thermalization(): host tables");
   if (gfx_set_links(g_ctx, (const double*)gf) != GFX_OK) {
     std::printf("Error in init_thermalization(): %s. Aborting...\n", gfx_last_error(g_ctx));
     std::exit(200);

@@ -52,6 +52,12 @@ extern gfx_thermparam_list thermparam;
 /* opaque handles of the context's device fields; pass them where the reference
  * passes dev_gf / dev_trafo1 (global.h:128, 140) */
 extern void *dev_gf, *dev_trafo1;
+/* host geometry tables (global.h:104-119), allocated and filled by init_gaugefixing
+ * and init_thermalization as the reference's initnn/initnn_eo do
+ * (cudagaugefix.cu:72-196, 285-323), freed by finalize_*: nn[8V] (+mu at 8 pos + mu,
+ * -mu at 8 pos + 4 + mu), ind[V], lexic2eo[V], nn_eo[4V], nn_oe[4V], eoidx_even[V/2],
+ * eoidx_odd[V/2].  The reference's host observables (observables.c) read nn. */
+extern int *nn, *ind, *lexic2eo, *nn_eo, *nn_oe, *eoidx_even, *eoidx_odd;
 
 /* cudagaugefix.cu:204 -- upload gf[4V] and trafo[V]; exit(100) on a bad volume,
  * exit(200) on allocation failure, as the reference */
@@ -83,6 +89,8 @@ void benchmark(void);
 /* No counterpart by name in the reference: the D2H copies its main does inline
  * (cudagaugefix.cu:785-793) and options the reference fixes at compile time. */
 int gfx_legacy_get_trafo(gfx_su3 *trafo);      /* g(x), V matrices */
+/* the geometry tables above for the current LX, LY, LZ, T (what init_* call); 0 or -1 */
+int gfx_legacy_init_tables(void);
 int gfx_legacy_get_gauge(gfx_su3 *gf);         /* current links, 4V matrices */
 void gfx_legacy_set_precision(int precision);  /* gfx_precision; default GFX_PREC_DOUBLE */
 void gfx_legacy_set_omega(double omega);       /* default 1.68 (overrelax.cu:416) */

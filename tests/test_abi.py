@@ -83,3 +83,31 @@ def test_sa_temperature_matches_reference_formulas(gfx):
         a = (Tmin ** -2.0 - Tmax ** -2.0) / (N - 1)
         assert sa_temperature(Tmin, Tmax, N, 2.0, i) == pytest.approx(
             (a * i + Tmax ** -2.0) ** (-1 / 2.0), rel=1e-14)
+
+
+def test_legacy_host_tables_match_reference_layout(gfx, oracle):
+    # the tables init_gaugefixing fills for the reference's host code (initnn and
+    # initnn_eo, cudagaugefix.cu:72-196): compared with the oracle's restatement
+    import ctypes
+    lib = gfx.lib
+    dims = (4, 6, 2, 8)
+    for name, v in zip(("LX", "LY", "LZ", "T"), dims):
+        ctypes.c_int.in_dll(lib, name).value = v
+    V = int(np.prod(dims))
+    assert lib.gfx_legacy_init_tables() == 0
+
+    def table(name, n):
+        p = ctypes.c_void_p.in_dll(lib, name).value
+        return np.ctypeslib.as_array((ctypes.c_int * n).from_address(p)).copy()
+
+    onn, oev, ood = oracle.lattice(dims)._keep
+    nn = table("nn", 8 * V)
+    assert np.array_equal(nn, onn)
+    even, odd = table("eoidx_even", V // 2), table("eoidx_odd", V // 2)
+    assert np.array_equal(even, oev) and np.array_equal(odd, ood)
+    assert np.array_equal(table("ind", V), np.arange(V))
+    l2e = table("lexic2eo", V)
+    assert np.array_equal(l2e[even], np.arange(V // 2)) and np.array_equal(l2e[odd], np.arange(V // 2))
+    nn_eo, nn_oe = table("nn_eo", 4 * V).reshape(-1, 8), table("nn_oe", 4 * V).reshape(-1, 8)
+    assert np.array_equal(nn_eo, l2e[nn.reshape(-1, 8)[even]])
+    assert np.array_equal(nn_oe, l2e[nn.reshape(-1, 8)[odd]])
