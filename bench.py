@@ -571,6 +571,9 @@ def run_gfx(args, dims):
     pin_out = gfx.pinned_empty(g0.shape)
     e2e_t, e2e_upd, e2e_dev = 0.0, 0, 0.0
     parts = {"set_links": 0.0, "set_trafo": 0.0, "overrelax": 0.0, "get_trafo": 0.0}
+    dev_parts = {k + s: 0.0 for k in ("set_links", "set_trafo", "get_trafo")
+                 for s in ("_copy", "_layout")}
+    io_direct = {}
     for _ in range(args.steps):
         ctx.synchronize()
         t0 = time.perf_counter()
@@ -585,6 +588,11 @@ def run_gfx(args, dims):
         e2e_t += t4 - t0
         e2e_upd += r.sweeps * V
         e2e_dev += r.ms / 1000.0
+        io = ctx.transfer_times()
+        for k, (cp, lay, direct) in io.items():
+            dev_parts[k + "_copy"] += cp / 1000.0
+            dev_parts[k + "_layout"] += lay / 1000.0
+            io_direct[k] = direct
         # each call returns after its work on the device is done
         parts["set_links"] += t1 - t0
         parts["set_trafo"] += t2 - t1
@@ -693,7 +701,11 @@ def run_gfx(args, dims):
                 # synchronizes before it returns); overrelax_host_s = its wall time
                 # outside the device-timed solve
                 "breakdown_s": dict({k: v / args.steps for k, v in parts.items()},
-                                    overrelax_host_s=(parts["overrelax"] - e2e_dev) / args.steps)},
+                                    overrelax_host_s=(parts["overrelax"] - e2e_dev) / args.steps),
+                # CUDA-event times per step of the transfers' copies and layout kernels
+                # (copy 0: the GPU reads / writes the page-locked host arrays directly)
+                "device_breakdown_s": {k: v / args.steps for k, v in dev_parts.items()},
+                "direct_host_access": io_direct},
         "clocks": clocks,
         "gpu_launches": int(launches),
         "gribov_batch": gribov,

@@ -379,6 +379,14 @@ class Context:
         self._check(lib.gfx_time_sweeps(self._h, n, omega, gauge, precision, _ptr(ms)))
         return float(ms[0])
 
+    def transfer_times(self):
+        """device ms of the last set_links / set_trafo / get_trafo: {name: (copy, layout,
+        direct)}; direct = the GPU used the gfx_host_alloc buffer itself"""
+        ms, d = np.zeros(6), (_I * 3)()
+        self._check(lib.gfx_transfer_times(self._h, _ptr(ms), d))
+        return {n: (float(ms[2 * k]), float(ms[2 * k + 1]), bool(d[k]))
+                for k, n in enumerate(("set_links", "set_trafo", "get_trafo"))}
+
     def set_fused_check(self, fused):
         self._check(lib.gfx_set_fused_check(self._h, 1 if fused else 0))
 
@@ -511,6 +519,7 @@ _sig("gfx_batch_random_haar", _I, [_V, _c.c_uint64])
 _sig("gfx_batch_random_haar_copy", _I, [_V, _I, _I, _c.c_uint64])
 _sig("gfx_batch_set_paired", _I, [_V, _I])
 _sig("gfx_set_fused_check", _I, [_V, _I])
+_sig("gfx_transfer_times", _I, [_V, _dp, _c.POINTER(_I)])
 _sig("gfx_batch_overrelax", _I, [_V, _c.POINTER(ORParams), _c.POINTER(CopyResult), _dp])
 _sig("gfx_batch_best", _I, [_V, _c.POINTER(CopyResult), _I, _c.POINTER(_I), _dp])
 _sig("gfx_random_trafo_haar", _I, [_V, _c.c_uint64])

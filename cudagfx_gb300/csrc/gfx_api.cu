@@ -9,6 +9,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <ctime>
 #include <functional>
 #include <string>
@@ -22,6 +24,35 @@
 using namespace gfx;
 
 static std::string g_global_err;
+
+// page-locked host allocations made by gfx_host_alloc: start -> size
+static std::mutex g_pinned_mu;
+static std::map<uintptr_t, size_t> g_pinned;
+
+namespace gfx {
+// The device address of [p, p + bytes) when that range lies in one gfx_host_alloc
+// allocation and p is 16-byte aligned (the tiled layout kernels move 16-byte words);
+// else nullptr and the caller stages through device memory.
+void* host_direct_ptr(const void* p, size_t bytes) {
+  const uintptr_t a = (uintptr_t)p;
+  if (a % 16) return nullptr;
+  uintptr_t base = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    auto it = g_pinned.upper_bound(a);
+    if (it == g_pinned.begin()) return nullptr;
+    --it;
+    if (a < it->first || a + bytes > it->first + it->second) return nullptr;
+    base = it->first;
+  }
+  void* d = nullptr;
+  if (cudaHostGetDevicePointer(&d, (void*)base, 0) != cudaSuccess || !d) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return (char*)d + (a - base);
+}
+}  // namespace gfx
 
 
 
@@ -326,6 +357,8 @@ gfx_status gfx_destroy(gfx_ctx* ctx) {
     if (p) cudaFree(p);
   if (ctx->loop_host) cudaFreeHost(ctx->loop_host);
   if (ctx->reduced_host) cudaFreeHost(ctx->reduced_host);
+  for (int k = 0; k < 3; k++)
+    if (ctx->io_ev[k]) cudaEventDestroy(ctx->io_ev[k]);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GFX_OK;
@@ -384,6 +417,18 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->gauss = ctx->unif = nullptr;
   ctx->dev_bytes = 0;
   ctx->launches = 0;
+  for (int k = 0; k < 3; k++) {
+    ctx->io_ev[k] = nullptr;
+    ctx->io_ms[k][0] = ctx->io_ms[k][1] = 0.0;
+    ctx->io_direct[k] = 0;
+  }
+  for (int k = 0; k < 3; k++)
+    if (cudaEventCreate(&ctx->io_ev[k]) != cudaSuccess) {
+      cudaGetLastError();
+      for (int j = 0; j < k; j++) cudaEventDestroy(ctx->io_ev[j]);
+      delete ctx;
+      return fail(nullptr, GFX_ERR_CUDA, "cudaEventCreate failed");
+    }
   gfx_status s;
   if (stream) {
     ctx->stream = (cudaStream_t)stream;
@@ -482,21 +527,55 @@ gfx_status gfx_set_block(gfx_ctx* ctx, int block) {
 // ---------------------------------------------------------------------------
 // fields
 // ---------------------------------------------------------------------------
+// Host arrays in page-locked memory from gfx_host_alloc: the layout kernels read and
+// write them directly (over the CPU-GPU link, coherent on Grace systems), so a host
+// transfer is one pass with no staging copy.  Other host memory goes through the
+// device scratch buffer with cudaMemcpyAsync.
+static gfx_status io_begin(gfx_ctx* ctx, int k) {
+  CK(cudaEventRecord(ctx->io_ev[0], ctx->stream));
+  ctx->io_direct[k] = 0;
+  return GFX_OK;
+}
+static gfx_status io_end(gfx_ctx* ctx, int k) {
+  CK(cudaEventRecord(ctx->io_ev[2], ctx->stream));
+  CK(cudaGetLastError());
+  CK(cudaEventSynchronize(ctx->io_ev[2]));
+  float a = 0.f, b = 0.f;
+  if (ctx->io_direct[k]) {
+    CK(cudaEventElapsedTime(&b, ctx->io_ev[0], ctx->io_ev[2]));
+  } else {
+    CK(cudaEventElapsedTime(&a, ctx->io_ev[0], ctx->io_ev[1]));
+    CK(cudaEventElapsedTime(&b, ctx->io_ev[1], ctx->io_ev[2]));
+  }
+  ctx->io_ms[k][0] = a;
+  ctx->io_ms[k][1] = b;
+  return GFX_OK;
+}
+
 gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
   if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_set_links: NULL argument");
   const size_t bytes = sizeof(double) * 18 * 4 * (size_t)ctx->vol;
-  gfx_status s = ensure_scratch(ctx, bytes);
+  gfx_status s = io_begin(ctx, 0);
   if (s) return s;
-  CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  launch_pack_links(ctx->link_nr, ctx->L, ctx->scratch_aos, ctx->U64, ctx->stream);
-  {
-    ctx->udf_valid = false;
+  const void* src = host_direct_ptr(su3, bytes);
+  if (!src) {
+    if ((s = ensure_scratch(ctx, bytes))) return s;
+    CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->io_ev[1], ctx->stream));
+    src = ctx->scratch_aos;
+  } else {
+    ctx->io_direct[0] = 1;
+  }
+  ctx->udf_valid = false;
+  // the FP32 12-real copy is written in the same pass (the 8-real one from U64 after)
+  const bool with32 = ctx->U32 && ctx->link_nr32 == 12;
+  launch_pack_links_tiled(ctx->link_nr, ctx->L, src, ctx->U64, with32 ? ctx->U32 : nullptr,
+                          ctx->stream);
+  if (ctx->U32 && !with32) {
     gfx_status rs = refresh_u32(ctx);
     if (rs) return rs;
   }
-  CK(cudaGetLastError());
-  CK(cudaStreamSynchronize(ctx->stream));
-  return GFX_OK;
+  return io_end(ctx, 0);
 }
 
 
@@ -516,27 +595,51 @@ gfx_status gfx_get_links(gfx_ctx* ctx, double* su3) {
 gfx_status gfx_set_trafo(gfx_ctx* ctx, const double* su3) {
   if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_set_trafo: NULL argument");
   const size_t bytes = sizeof(double) * 18 * (size_t)ctx->vol;
-  gfx_status s = ensure_scratch(ctx, bytes);
+  gfx_status s = io_begin(ctx, 1);
   if (s) return s;
-  CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
-  launch_pack_g(1, ctx->L, ctx->scratch_aos, ctx->G64, ctx->stream);
-  CK(cudaGetLastError());
+  const void* src = host_direct_ptr(su3, bytes);
+  if (!src) {
+    if ((s = ensure_scratch(ctx, bytes))) return s;
+    CK(cudaMemcpyAsync(ctx->scratch_aos, su3, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->io_ev[1], ctx->stream));
+    src = ctx->scratch_aos;
+  } else {
+    ctx->io_direct[1] = 1;
+  }
+  launch_pack_g_tiled(ctx->L, src, ctx->G64, ctx->stream);
   ctx->g_active = 1;
-  CK(cudaStreamSynchronize(ctx->stream));
-  return GFX_OK;
+  return io_end(ctx, 1);
 }
 
 gfx_status gfx_get_trafo(gfx_ctx* ctx, double* su3) {
   if (!ctx || !su3) return fail(ctx, GFX_ERR_ARG, "gfx_get_trafo: NULL argument");
   const size_t bytes = sizeof(double) * 18 * (size_t)ctx->vol;
-  gfx_status s = ensure_scratch(ctx, bytes);
+  gfx_status s = io_begin(ctx, 2);
   if (s) return s;
-  s = sync_g64(ctx);
-  if (s) return s;
-  launch_unpack_g(1, ctx->L, ctx->G64, ctx->scratch_aos, ctx->stream);
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(su3, ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  if ((s = sync_g64(ctx))) return s;
+  void* dst = host_direct_ptr(su3, bytes);
+  if (dst) {
+    ctx->io_direct[2] = 1;
+    launch_unpack_g_tiled(ctx->L, ctx->G64, dst, ctx->stream);
+  } else {
+    if ((s = ensure_scratch(ctx, bytes))) return s;
+    launch_unpack_g_tiled(ctx->L, ctx->G64, ctx->scratch_aos, ctx->stream);
+    // here the layout kernel comes first: [0] is the copy, so time it second
+    CK(cudaEventRecord(ctx->io_ev[1], ctx->stream));
+    CK(cudaMemcpyAsync(su3, ctx->scratch_aos, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  s = io_end(ctx, 2);
+  if (s == GFX_OK && !ctx->io_direct[2]) std::swap(ctx->io_ms[2][0], ctx->io_ms[2][1]);
+  return s;
+}
+
+gfx_status gfx_transfer_times(const gfx_ctx* ctx, double* ms, int* direct) {
+  if (!ctx || !ms) return fail(nullptr, GFX_ERR_ARG, "gfx_transfer_times: NULL argument");
+  for (int k = 0; k < 3; k++) {
+    ms[2 * k] = ctx->io_ms[k][0];
+    ms[2 * k + 1] = ctx->io_ms[k][1];
+    if (direct) direct[k] = ctx->io_direct[k];
+  }
   return GFX_OK;
 }
 
@@ -1297,11 +1400,18 @@ void* gfx_host_alloc(size_t bytes) {
     cudaGetLastError();
     return nullptr;
   }
+  std::lock_guard<std::mutex> lk(g_pinned_mu);
+  g_pinned[(uintptr_t)p] = bytes;
   return p;
 }
 
 void gfx_host_free(void* p) {
-  if (p) cudaFreeHost(p);
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned.erase((uintptr_t)p);
+  }
+  cudaFreeHost(p);
 }
 
 }  // extern "C"

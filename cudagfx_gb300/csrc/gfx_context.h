@@ -79,6 +79,12 @@ struct gfx_ctx {
   std::vector<gfx::CheckRecord> last_hist;
   size_t dev_bytes;
   unsigned long long launches;  // kernels enqueued by this context (graph bodies included)
+  // device times of the last set_links, set_trafo, get_trafo: [k][0] the host<->device
+  // copy (0 when the GPU reached the caller's page-locked buffer directly), [k][1] the
+  // layout kernels; io_direct[k] = 1 for the direct path
+  cudaEvent_t io_ev[3];
+  double io_ms[3][2];
+  int io_direct[3];
   std::string err;
 };
 
@@ -93,6 +99,9 @@ struct gfx_ctx {
 
 namespace gfx {
 
+// the device address of caller memory inside one gfx_host_alloc allocation (16-byte
+// aligned), or nullptr
+void* host_direct_ptr(const void* p, size_t bytes);
 // record msg as the context's and the library's last error; returns s
 gfx_status fail(gfx_ctx* ctx, gfx_status s, const std::string& msg);
 const std::string& global_error();

@@ -96,6 +96,13 @@ void launch_pack_links(int link_nr_prec, const Lattice& L, const double* aos, vo
 void launch_unpack_links(int link_nr_prec, const Lattice& L, const void* U, double* aos,
                          cudaStream_t s);
 void launch_pack_g(int gprec, const Lattice& L, const double* aos, void* G, cudaStream_t s);
+// the same by coalesced tiles; aos 16-byte aligned, in device memory or in page-locked
+// host memory the device reaches (its device address).  Links: FP64 planes of link_nr
+// reals and, when U32 is given, the FP32 12-real copy in the same pass
+void launch_pack_links_tiled(int link_nr, const Lattice& L, const void* aos, void* U64, void* U32,
+                             cudaStream_t s);
+void launch_pack_g_tiled(const Lattice& L, const void* aos, void* G64, cudaStream_t s);
+void launch_unpack_g_tiled(const Lattice& L, const void* G64, void* aos, cudaStream_t s);
 void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cudaStream_t s);
 // double-float copies of the links (18 reals) and of g (12 reals; to_df = 0 back to FP64)
 void launch_convert_links_64_to_df(int link_nr, const Lattice& L, const void* U64, void* Udf,

@@ -532,6 +532,96 @@ void launch_unpack_g(int gprec, const Lattice& L, const void* G, double* aos, cu
   else unpack_g_kernel<double><<<grid, 128, 0, s>>>(L, (const double2*)G, aos);
 }
 
+// ---------------------------------------------------------------------------
+// The same conversions by tiles, coalesced on both sides.  LX is even, so the
+// lexicographic site pos has eo index pos >> 1 in its parity: a block takes the eo
+// indices j0 .. j0 + kTileEo - 1 of both parities, which are exactly the 2 kTileEo
+// consecutive sites 2 j0 .. of the host order.  That AoS range is moved with
+// consecutive 16-byte accesses through shared memory -- from or to device memory, or
+// page-locked host memory that the GPU reaches directly (the host copy and the
+// layout change are then one pass) -- and each thread moves one matrix between the
+// tile and the even/odd planes.  Needs a 16-byte aligned AoS pointer.
+// ---------------------------------------------------------------------------
+constexpr int kTileEo = 32;
+
+// links (NMAT 4, link 4 pos + mu) or g (NMAT 1): AoS -> FP64 planes of NR reals, and
+// with W32 the FP32 12-real copy (the rounding of rows 0, 1, as links_64_to_32_kernel)
+template <int NMAT, int NR, bool W32>
+__global__ void __launch_bounds__(128) pack_tile_kernel(Lattice L, const double2* __restrict__ aos,
+                                                        double2* F64, float4* F32) {
+  extern __shared__ double2 tile[];
+  const int j0 = blockIdx.x * kTileEo;
+  const int nj = min(kTileEo, L.vh - j0);
+  const int n = 2 * nj * NMAT * 9;
+  const double2* src = aos + (size_t)2 * j0 * NMAT * 9;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) tile[k] = src[k];
+  __syncthreads();
+  constexpr int NC = Field<double, NR>::NCHUNK;
+  const size_t vh = (size_t)L.vh;
+  for (int k = threadIdx.x; k < 2 * NMAT * nj; k += blockDim.x) {
+    const int j = k % nj, pm = k / nj, parity = pm / NMAT, mu = pm - parity * NMAT;
+    const Site c = site_of(L, j0 + j, parity);
+    const double2* m = tile + ((2 * j + c.s) * NMAT + mu) * 9;
+    Mat3<double> d;
+#pragma unroll
+    for (int e = 0; e < 9; e++) d.e[e / 3][e % 3] = cmk<double>(m[e].x, m[e].y);
+    Field<double, NR>::store(F64 + (size_t)(parity * NMAT + mu) * NC * vh, vh, j0 + j, d);
+    if (W32) {
+      Mat3<float> f;
+#pragma unroll
+      for (int r = 0; r < 2; r++)
+#pragma unroll
+        for (int e = 0; e < 3; e++)
+          f.e[r][e] = cmk<float>((float)d.e[r][e].re, (float)d.e[r][e].im);
+      Field<float, 12>::store(F32 + (size_t)(parity * NMAT + mu) * 3 * vh, vh, j0 + j, f);
+    }
+  }
+}
+
+// FP64 12-real g planes -> AoS su3 (row 2 rebuilt, as unpack_g_kernel<double>)
+__global__ void __launch_bounds__(128) unpack_g_tile_kernel(Lattice L, const double2* G,
+                                                            double2* __restrict__ aos) {
+  __shared__ double2 tile[2 * kTileEo * 9];
+  const int j0 = blockIdx.x * kTileEo;
+  const int nj = min(kTileEo, L.vh - j0);
+  const size_t vh = (size_t)L.vh;
+  for (int k = threadIdx.x; k < 2 * nj; k += blockDim.x) {
+    const int j = k % nj, parity = k / nj;
+    const Site c = site_of(L, j0 + j, parity);
+    Mat3<double> m;
+    Field<double, 12>::load(G + (size_t)parity * 6 * vh, vh, j0 + j, m);
+    double2* o = tile + (2 * j + c.s) * 9;
+#pragma unroll
+    for (int e = 0; e < 9; e++) o[e] = make_double2(m.e[e / 3][e % 3].re, m.e[e / 3][e % 3].im);
+  }
+  __syncthreads();
+  double2* dst = aos + (size_t)2 * j0 * 9;
+  for (int k = threadIdx.x; k < 2 * nj * 9; k += blockDim.x) dst[k] = tile[k];
+}
+
+void launch_pack_links_tiled(int link_nr, const Lattice& L, const void* aos, void* U64, void* U32,
+                             cudaStream_t s) {
+  const int grid = (L.vh + kTileEo - 1) / kTileEo;
+  const size_t sm = sizeof(double2) * 2 * kTileEo * 4 * 9;
+  const double2* a = (const double2*)aos;
+  if (link_nr == 18) {
+    if (U32) pack_tile_kernel<4, 18, true><<<grid, 128, sm, s>>>(L, a, (double2*)U64, (float4*)U32);
+    else pack_tile_kernel<4, 18, false><<<grid, 128, sm, s>>>(L, a, (double2*)U64, nullptr);
+  } else {
+    if (U32) pack_tile_kernel<4, 12, true><<<grid, 128, sm, s>>>(L, a, (double2*)U64, (float4*)U32);
+    else pack_tile_kernel<4, 12, false><<<grid, 128, sm, s>>>(L, a, (double2*)U64, nullptr);
+  }
+}
+void launch_pack_g_tiled(const Lattice& L, const void* aos, void* G64, cudaStream_t s) {
+  const int grid = (L.vh + kTileEo - 1) / kTileEo;
+  pack_tile_kernel<1, 12, false><<<grid, 128, sizeof(double2) * 2 * kTileEo * 9, s>>>(
+      L, (const double2*)aos, (double2*)G64, nullptr);
+}
+void launch_unpack_g_tiled(const Lattice& L, const void* G64, void* aos, cudaStream_t s) {
+  const int grid = (L.vh + kTileEo - 1) / kTileEo;
+  unpack_g_tile_kernel<<<grid, 128, 0, s>>>(L, (const double2*)G64, (double2*)aos);
+}
+
 // FP32 copy of the links: 12 reals (rows 0, 1) or 8 (a2, a3, arg a1, arg c1, b1; the
 // angles by atan2 in FP64 as su3to8 does, su3manip.c:234-253)
 template <int NR, int NR32>

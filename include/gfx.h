@@ -248,6 +248,10 @@ gfx_status gfx_functional_noalloc(const void *links_device, const void *trafo_de
                                   int ly, int lz, int lt, int link_reals, int gauge,
                                   double *result_device, void *stream);
 
+/* device times (ms) of the last gfx_set_links, gfx_set_trafo and gfx_get_trafo: ms[2k]
+ * the host<->device copy, ms[2k+1] the layout kernels; direct[k] = 1 when the GPU read
+ * or wrote the caller's gfx_host_alloc buffer itself (no copy) */
+gfx_status gfx_transfer_times(const gfx_ctx *ctx, double *ms, int *direct);
 /* FP32 convergence checks fused into the last odd half-sweep before the check (1, the
  * default; used when the FP32 links hold 12 reals and each time slice holds whole
  * 128-site blocks of each parity) or a separate measurement (0); the check values are
@@ -341,6 +345,8 @@ gfx_status gfx_random_trafo_haar(gfx_ctx *ctx, uint64_t seed);
 
 /* ---- host-side helpers ---- */
 /* page-locked host memory for the field copies (cudaMallocHost); NULL on failure */
+/* Page-locked host memory.  Field arrays in it (gfx_set_links, gfx_set_trafo,
+ * gfx_get_trafo) are read or written by the GPU directly, with no staging copy. */
 void *gfx_host_alloc(size_t bytes);
 void gfx_host_free(void *p);
 /* glibc srand(seed)/rand() stream */

@@ -156,8 +156,10 @@ def build_reference_link():
     main = os.path.join(HERE, "ref_link_main.c")
     if _newer(REF_PROGRAM, srcs + [main, libgfx, __file__]):
         inc = ["-I" + REFERENCE, "-I" + os.path.join(repo, "include"), "-I/usr/local/cuda/include"]
-        _run(["gcc", "-O2", "-w", "-std=gnu99"] + inc + srcs + [main, "-o", REF_PROGRAM,
-             "-L" + pkg, "-lgfx", "-Wl,-rpath," + pkg, "-lm"])
+        # -ffp-contract=off: aarch64 gcc fuses a*b+c into FMA by default, x86-64 without
+        # -march does not; with it off both give the reference's random start bit for bit
+        _run(["gcc", "-O2", "-w", "-std=gnu99", "-ffp-contract=off"] + inc + srcs +
+             [main, "-o", REF_PROGRAM, "-L" + pkg, "-lgfx", "-Wl,-rpath," + pkg, "-lm"])
     return REF_PROGRAM
 
 
