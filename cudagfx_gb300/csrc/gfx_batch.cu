@@ -31,8 +31,11 @@ constexpr int kMaxConf = 8;
 struct BConf {
   Lattice L;
   const void* U32;   // FP32 12-real links
+  void* U32P;        // the same links in both lanes of the pair layout (P12)
   const void* U64;   // FP64 12-real links
-  void* G32;         // copy 0's g (FP32), copy k at + k * gstride32 vectors
+  void* G32;         // copy 0's g (FP32), copy k at + k * gstride32 vectors; while the
+                     // FP32 sweeps run two copies per thread, pair k (copies 2k, 2k+1)
+                     // in the P12 layout at + 2 k * gstride32
   void* G64;         // copy 0's g (FP64), copy k at + k * gstride64 vectors
   size_t gstride32, gstride64;
   void* Ur;          // rebased FP32 polish (polish = 2): copy k's rebased links at
@@ -55,6 +58,7 @@ struct BDesc {
   BConf c[kMaxConf];
   int nconf;
   int ncopies;  // all configurations
+  int paired;   // FP32 g of the sweeps in the pair layout (or_batch_pair_kernel)
   LoopState* states;
   double* partials;
   double* slice_sums;
@@ -95,8 +99,10 @@ __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_
 // The FP32 half-sweep with two copies per thread (or_site_update_pair: packed FP32
 // arithmetic, lane for lane the operations of or_batch_kernel<float>).  Work items are
 // (configuration, site block, copy pair), pair-minor, so the pairs of a site block run
-// side by side as in or_batch_kernel; each thread loads its 8 links once for both
-// copies.  A pair with one finished copy runs the other copy in both lanes.
+// side by side as in or_batch_kernel.  The pair's g and the links (held in both lanes)
+// are in the P12 layout, so every operand of the packed instructions comes straight
+// from a 16-byte load.  The second lane of a configuration's last pair when its copy
+// count is odd holds a duplicate of the first and is never written.
 template <int NDIR>
 __global__ void __launch_bounds__(kBatchBlock, 4) or_batch_pair_kernel(BDesc d, int parity,
                                                                        float omega) {
@@ -105,17 +111,33 @@ __global__ void __launch_bounds__(kBatchBlock, 4) or_batch_pair_kernel(BDesc d, 
   const BConf& C = d.c[ci];
   const int local = item - C.pitem_base;
   const int blk = local / C.npairs, pair = local - blk * C.npairs;
-  const int c0 = 2 * pair, c1 = min(c0 + 1, C.ncopies - 1);
+  const int c0 = 2 * pair, c1 = c0 + 1;
   const bool run0 = d.states[C.copy_base + c0].done == 0;
-  const bool run1 = d.states[C.copy_base + c1].done == 0;
+  const bool run1 = c1 < C.ncopies && d.states[C.copy_base + c1].done == 0;
   if (!run0 && !run1) return;  // uniform over the block
   const int i = blk * kBatchBlock + threadIdx.x;
   if (i >= C.L.vh) return;
-  float4* G = (float4*)C.G32;
-  float4* Ga = G + (size_t)(run0 ? c0 : c1) * C.gstride32;
-  float4* Gb = G + (size_t)(run1 ? c1 : c0) * C.gstride32;
-  or_site_update_pair<NDIR>(C.L, site_of(C.L, i, parity), parity, (const float4*)C.U32, Ga, Gb,
-                            i, omega);
+  P12 U, G;
+  U.p = (float4*)C.U32P;
+  G.p = (float4*)C.G32 + (size_t)c0 * C.gstride32;
+  or_site_update_pair<NDIR>(C.L, site_of(C.L, i, parity), parity, U, G, i, omega, run0, run1);
+}
+
+// the FP32 links of configuration conf in both lanes of the pair layout
+__global__ void links_pair_kernel(BDesc d, int conf) {
+  const BConf& C = d.c[conf];
+  const int blk = blockIdx.y;  // parity * 4 + mu
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= C.L.vh) return;
+  const size_t vh = (size_t)C.L.vh;
+  Mat3<float> f;
+  Field<float, 12>::load((const float4*)C.U32 + (size_t)blk * 3 * vh, vh, i, f);
+  float4* o = (float4*)C.U32P + (size_t)blk * kPairPlanes * vh;
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    const cplx<float> z = f.e[e / 3][e % 3];
+    o[e * vh + i] = make_float4(z.re, z.re, z.im, z.im);
+  }
 }
 
 // The rebased FP32 polish sweep for all active copies (or_rebased_kernel per copy, the
@@ -162,15 +184,30 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
   if (k < C.L.st) {
     const int i = t * C.L.st + k;
     const Site c = site_of(C.L, i, parity);
+    const size_t vh = (size_t)C.L.vh;
     Mat3<TC> star, g;
-    if constexpr (F32)
-      compute_star_f32<NDIR>(C.L, c, parity, (const float4*)U, (const float4*)G, star);
-    else
+    if constexpr (F32) {
+      if (d.paired) {
+        // this copy's lane of its pair (P12 layout)
+        LaneP12 Gl;
+        Gl.p = (const float4*)C.G32 + (size_t)(copy & ~1) * C.gstride32;
+        Gl.lane = copy & 1;
+        Mat3<float> s, h;
+        compute_star_12<float, const float4*, LaneP12, NDIR>(C.L, c, parity, (const float4*)U,
+                                                               Gl, s);
+        g_full(Gl + (size_t)parity * kPairPlanes * vh, vh, i, h);
+        site_functional_f32(h, s, f32, d32);
+      } else {
+        compute_star_f32<NDIR>(C.L, c, parity, (const float4*)U, (const float4*)G, star);
+        Load<TC, TSG, 12>::go(G + (size_t)parity * 3 * vh, vh, i, g);
+        site_functional_f32(g, star, f32, d32);
+      }
+    } else {
       compute_star<TC, TC, 12, TSG, 12, NDIR>(C.L, c, parity, U, G, star);
-    constexpr int NCG = Field<TSG, 12>::NCHUNK;
-    Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * C.L.vh, (size_t)C.L.vh, i, g);
-    if constexpr (F32) site_functional_f32(g, star, f32, d32);
-    else site_functional(g, star, f, dd);
+      constexpr int NCG = Field<TSG, 12>::NCHUNK;
+      Load<TC, TSG, 12>::go(G + (size_t)parity * NCG * vh, vh, i, g);
+      site_functional(g, star, f, dd);
+    }
   }
   double* out = d.partials +
                 3 * (C.part_base + (size_t)copy * per_copy + (size_t)(parity * C.L.lt + t) * C.nbx + bx);
@@ -264,10 +301,27 @@ __global__ void convert_batch_kernel(BDesc d, int to64, int only_state) {
   const size_t vh = (size_t)C.L.vh;
   for (int parity = 0; parity < 2; parity++) {
     const float4* g32 = (const float4*)C.G32 + (size_t)copy * C.gstride32 + (size_t)parity * 3 * vh;
+    // the pair layout: this copy's lane of pair copy / 2
+    float* g32p = (float*)((float4*)C.G32 + (size_t)(copy & ~1) * C.gstride32 +
+                           (size_t)parity * kPairPlanes * vh);
+    const int lane = copy & 1;
     const double2* g64 = (const double2*)C.G64 + (size_t)copy * C.gstride64 + (size_t)parity * 6 * vh;
     if (to64) {
       Mat3<double> m;
-      Load<double, float, 12>::go(g32, vh, i, m);
+      if (d.paired) {
+        LaneP12 Gl;
+        Gl.p = (const float4*)g32p;
+        Gl.lane = lane;
+        Mat3<float> f;
+        load12_rows01(Gl, vh, i, f);
+#pragma unroll
+        for (int r = 0; r < 2; r++)
+#pragma unroll
+          for (int c = 0; c < 3; c++) m.e[r][c] = cmk<double>(f.e[r][c].re, f.e[r][c].im);
+        normalize<double, true>(m);  // as Load<double, float, 12>
+      } else {
+        Load<double, float, 12>::go(g32, vh, i, m);
+      }
       Field<double, 12>::store((double2*)g64, vh, i, m);
     } else {
       Mat3<double> m;
@@ -277,7 +331,22 @@ __global__ void convert_batch_kernel(BDesc d, int to64, int only_state) {
       for (int r = 0; r < 3; r++)
 #pragma unroll
         for (int c = 0; c < 3; c++) f.e[r][c] = cmk<float>((float)m.e[r][c].re, (float)m.e[r][c].im);
-      Field<float, 12>::store((float4*)g32, vh, i, f);
+      if (d.paired) {
+        // the last copy of an odd count also fills the unused second lane
+        const bool both = lane == 0 && copy + 1 == C.ncopies;
+#pragma unroll
+        for (int e = 0; e < 6; e++) {
+          float* q = g32p + 4 * (e * vh + i);
+          q[lane] = f.e[e / 3][e % 3].re;
+          q[2 + lane] = f.e[e / 3][e % 3].im;
+          if (both) {
+            q[1] = f.e[e / 3][e % 3].re;
+            q[3] = f.e[e / 3][e % 3].im;
+          }
+        }
+      } else {
+        Field<float, 12>::store((float4*)g32, vh, i, f);
+      }
     }
   }
 }
@@ -593,7 +662,10 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     if (precision != GFX_PREC_DOUBLE) {
       BTRY(balloc(b, &p, (size_t)8 * 3 * 16 * vh));
       C.U32 = p;
-      BTRY(balloc(b, &p, (size_t)C.ncopies * C.gstride32 * 16));
+      BTRY(balloc(b, &p, (size_t)8 * kPairPlanes * 16 * vh));
+      C.U32P = p;
+      // whole pairs: the pair layout of the FP32 sweeps fills 2 * npairs copy slots
+      BTRY(balloc(b, &p, (size_t)2 * C.npairs * C.gstride32 * 16));
       C.G32 = p;
     }
     copy_base += C.ncopies;
@@ -608,6 +680,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
   b->nitems = item;
   b->npitems = pitem;
   b->paired = 0;
+  b->desc.paired = 0;
   b->nmitems = mitem;
   b->nsitems = sitem;
   b->desc.nconf = nconf;
@@ -637,7 +710,7 @@ int gfx_batch_copies(const gfx_batch* b) { return b ? b->ncopies : 0; }
 
 gfx_status gfx_batch_set_paired(gfx_batch* b, int paired) {
   if (!b) return bfail(nullptr, GFX_ERR_ARG, "NULL batch");
-  paired = paired ? 1 : 0;
+  paired = paired && b->precision != GFX_PREC_DOUBLE ? 1 : 0;
   if (paired == b->paired) return GFX_OK;
   BCK(cudaStreamSynchronize(b->stream));
   for (auto& g : b->graphs) {  // captured with the other sweep kernel
@@ -646,6 +719,7 @@ gfx_status gfx_batch_set_paired(gfx_batch* b, int paired) {
   }
   b->graphs.clear();
   b->paired = paired;
+  b->desc.paired = paired;  // the FP32 g layout: each solve converts into it at its start
   return GFX_OK;
 }
 
@@ -663,7 +737,10 @@ gfx_status gfx_batch_set_links(gfx_batch* b, int conf, const double* su3) {
   BCK(cudaMallocAsync((void**)&scratch, bytes, b->stream));
   BCK(cudaMemcpyAsync(scratch, su3, bytes, cudaMemcpyHostToDevice, b->stream));
   launch_pack_links(12, C.L, scratch, (void*)C.U64, b->stream);
-  if (C.U32) launch_convert_links_64_to_32(12, 12, C.L, C.U64, (void*)C.U32, b->stream);
+  if (C.U32) {
+    launch_convert_links_64_to_32(12, 12, C.L, C.U64, (void*)C.U32, b->stream);
+    links_pair_kernel<<<dim3((C.L.vh + 127) / 128, 8), 128, 0, b->stream>>>(b->desc, conf);
+  }
   BCK(cudaFreeAsync(scratch, b->stream));
   BCK(cudaGetLastError());
   BCK(cudaStreamSynchronize(b->stream));

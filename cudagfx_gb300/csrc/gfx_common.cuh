@@ -166,8 +166,9 @@ __device__ __forceinline__ void acc_cross(cplx<T>& acc, cplx<T> p, cplx<T> q, cp
   acc.im = fm(p.re, q.im, fm(p.im, q.re, fm(-r.re, s.im, fm(-r.im, s.re, acc.im))));
 }
 
-// link loads of the FP32 star: scalar for one copy; for two copies in a thread (T = f2,
-// gfx_pair.cuh) the link is loaded once and broadcast to both lanes
+// loads of the FP32 star.  Scalar: one copy, 3 planes of float4 per matrix.  Pairs
+// (T = f2, gfx_pair.cuh): the P12 layout, 6 planes per matrix, for the two copies' g
+// and for the links held in both lanes; LaneP12 reads one copy of a pair field.
 __device__ __forceinline__ void link_rows01(const float4* base, size_t stride, int i,
                                             Mat3<float>& m) {
   load12_rows01(base, stride, i, m);
@@ -176,48 +177,57 @@ __device__ __forceinline__ void link_full(const float4* base, size_t stride, int
                                           Mat3<float>& m) {
   Field<float, 12>::load(base, stride, i, m);
 }
-__device__ __forceinline__ void g_rows01(const float4* base, size_t stride, int i,
-                                         Mat3<float>& m) {
+template <typename P, typename M>
+__device__ __forceinline__ void g_rows01(const P& base, size_t stride, int i, M& m) {
   load12_rows01(base, stride, i, m);
 }
 __device__ __forceinline__ void g_full(const float4* base, size_t stride, int i, Mat3<float>& m) {
   Field<float, 12>::load(base, stride, i, m);
 }
-__device__ __forceinline__ void link_rows01(const float4* base, size_t stride, int i,
-                                            Mat3<f2>& m) {
-  Mat3<float> s;
-  load12_rows01(base, stride, i, s);
-  broadcast(s, m, 2);
+__device__ __forceinline__ void g_full(const LaneP12& base, size_t stride, int i,
+                                       Mat3<float>& m) {
+  load12_rows01(base, stride, i, m);
+  row2_from_01(m);
 }
-__device__ __forceinline__ void link_full(const float4* base, size_t stride, int i, Mat3<f2>& m) {
-  Mat3<float> s;
-  Field<float, 12>::load(base, stride, i, s);
-  broadcast(s, m, 3);
-}
-__device__ __forceinline__ void g_rows01(const GPairPtr& base, size_t stride, int i,
-                                         Mat3<f2>& m) {
+__device__ __forceinline__ void link_rows01(const P12& base, size_t stride, int i, Mat3<f2>& m) {
   load12_rows01(base, stride, i, m);
 }
-__device__ __forceinline__ void g_full(const GPairPtr& base, size_t stride, int i, Mat3<f2>& m) {
+__device__ __forceinline__ void link_full(const P12& base, size_t stride, int i, Mat3<f2>& m) {
   load12(base, stride, i, m);
 }
+__device__ __forceinline__ void g_full(const P12& base, size_t stride, int i, Mat3<f2>& m) {
+  load12(base, stride, i, m);
+}
+template <typename P>
+struct Planes {
+  static constexpr int n = 3;
+};
+template <>
+struct Planes<P12> {
+  static constexpr int n = kPairPlanes;
+};
+template <>
+struct Planes<LaneP12> {
+  static constexpr int n = kPairPlanes;
+};
 
-// T = float with GP = const float4* (one copy), or T = f2 with GP = GPairPtr (two copies
-// of one configuration; the same operations lane for lane)
-template <typename T, typename GP, int NDIR>
+// T = float with UP = GP = const float4* (one copy) or GP = LaneP12 (one copy of a pair
+// field), or T = f2 with UP = GP = P12 (two copies of one configuration): the same
+// operations lane for lane
+template <typename T, typename UP, typename GP, int NDIR>
 __device__ __forceinline__ void compute_star_12(const Lattice& L, const Site& c, int parity,
-                                                const float4* __restrict__ U, GP G,
-                                                Mat3<T>& star) {
+                                                UP U, GP G, Mat3<T>& star) {
+  constexpr int NPU = Planes<UP>::n, NPG = Planes<GP>::n;
   const size_t vh = (size_t)L.vh;
   const int q = 1 - parity;
-  const GP Gq = G + (size_t)q * 3 * vh;
+  const GP Gq = G + (size_t)q * NPG * vh;
   mzero(star);
 #pragma unroll
   for (int mu = 0; mu < NDIR; mu++) {
     Mat3<T> a, b;
     cplx<T> P[2][3];
     // forward: P = U g^+
-    link_rows01(U + (size_t)(parity * 4 + mu) * 3 * vh, vh, c.i, a);
+    link_rows01(U + (size_t)(parity * 4 + mu) * NPU * vh, vh, c.i, a);
     g_full(Gq, vh, nb_fwd(L, c, mu), b);
 #pragma unroll
     for (int r = 0; r < 2; r++)
@@ -235,7 +245,7 @@ __device__ __forceinline__ void compute_star_12(const Lattice& L, const Site& c,
     // backward: Q = g(x-mu) U_mu(x-mu), w += Q^+
     const int jb = nb_bwd(L, c, mu);
     g_rows01(Gq, vh, jb, b);
-    link_full(U + (size_t)(q * 4 + mu) * 3 * vh, vh, jb, a);
+    link_full(U + (size_t)(q * 4 + mu) * NPU * vh, vh, jb, a);
 #pragma unroll
     for (int r = 0; r < 2; r++)
 #pragma unroll
@@ -258,7 +268,7 @@ __device__ __forceinline__ void compute_star_f32(const Lattice& L, const Site& c
                                                  const float4* __restrict__ U,
                                                  const float4* __restrict__ G,
                                                  Mat3<float>& star) {
-  compute_star_12<float, const float4*, NDIR>(L, c, parity, U, G, star);
+  compute_star_12<float, const float4*, const float4*, NDIR>(L, c, parity, U, G, star);
 }
 
 // One overrelaxation site update (overrelax.cu:335-446) of site i of parity `parity`
@@ -290,21 +300,20 @@ __device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, 
 }
 
 // The FP32 update of site i for two copies of one configuration at once (T = f2):
-// lane for lane the operations of or_site_update<float, 12, NDIR>.  Ga, Gb: the two
-// copies' g fields (Ga == Gb runs one copy twice, which stores the same values twice).
+// lane for lane the operations of or_site_update<float, 12, NDIR>.  U: the links in
+// both lanes, G: the pair's g, both in the P12 layout.  A lane whose copy has stopped
+// (run_x / run_y false) is computed but its stored bits are written back unchanged.
 template <int NDIR>
 __device__ __forceinline__ void or_site_update_pair(const Lattice& L, const Site& c, int parity,
-                                                    const float4* __restrict__ U, float4* Ga,
-                                                    float4* Gb, int i, float omega) {
+                                                    P12 U, P12 G, int i, float omega, bool run_x,
+                                                    bool run_y) {
   const size_t vh = (size_t)L.vh;
-  GPairPtr G;
-  G.a = Ga;
-  G.b = Gb;
   Mat3<f2> star, gold, gn;
-  compute_star_12<f2, GPairPtr, NDIR>(L, c, parity, U, G, star);
-  load12(G + (size_t)parity * 3 * vh, vh, i, gold);
+  compute_star_12<f2, P12, P12, NDIR>(L, c, parity, U, G, star);
+  const P12 Gp = G + (size_t)parity * kPairPlanes * vh;
+  load12(Gp, vh, i, gold);
   or_update_composed(gold, star, f2(omega), gn);
-  store12(Ga + (size_t)parity * 3 * vh, Gb + (size_t)parity * 3 * vh, vh, i, gn);
+  store12(Gp, vh, i, gn, gold, !run_x, !run_y);
 }
 
 // Per-site functional from X = g w (overrelax.cu:451-605, see measure_kernel):

@@ -8,7 +8,8 @@
 // gfx_device.cuh and gfx_common.cuh instantiated with T = f2 therefore gives, lane
 // for lane, the bits of the scalar FP32 kernels (the scalar code uses no contracted
 // a*b+c: every FMA is an explicit fm()), at about half the instruction issue.  The
-// links, shared by both copies, are loaded once and broadcast to both lanes.
+// fields are kept in a pair layout (P12 below) so that the packed operands come
+// straight from 16-byte loads, with no register moves to pair them up.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -49,72 +50,68 @@ __device__ __forceinline__ f2 rsqrt_t<f2>(f2 x) {
   return f2(rsqrtf(x.v.x), rsqrtf(x.v.y));
 }
 
-// a pair of gauge-transformation fields: the two copies' FP32 12-real fields
-struct GPairPtr {
-  const float4* a;
-  const float4* b;
-  __device__ __forceinline__ GPairPtr operator+(size_t off) const {
-    GPairPtr r;
-    r.a = a + off;
-    r.b = b + off;
+// The pair layout of an FP32 12-real field: plane e (e = 0..5, the complex entries of
+// rows 0 and 1) holds, per site, the float4 {re of lane x, re of lane y, im of lane x,
+// im of lane y}.  One 16-byte load then fills cplx<f2> in register pairs as the packed
+// instructions take them.  A pair of gauge copies stores its two g this way (6 planes
+// per parity); a link field shared by both copies stores each link in both lanes.
+struct P12 {
+  float4* p;
+  __device__ __forceinline__ P12 operator+(size_t off) const {
+    P12 r;
+    r.p = p + off;
     return r;
   }
 };
+constexpr int kPairPlanes = 6;
 
-__device__ __forceinline__ cplx<f2> cpair(float ar, float ai, float br, float bi) {
-  cplx<f2> z;
-  z.re = f2(ar, br);
-  z.im = f2(ai, bi);
-  return z;
-}
-
-// rows 0,1 of both copies' g at site i (planes spaced by stride)
-__device__ __forceinline__ void load12_rows01(const GPairPtr& base, size_t stride, int i,
+// rows 0,1 of the pair at site i (planes spaced by stride)
+__device__ __forceinline__ void load12_rows01(const P12& base, size_t stride, int i,
                                               Mat3<f2>& m) {
-  const float4 a0 = __ldg(base.a + i), a1 = __ldg(base.a + stride + i),
-               a2 = __ldg(base.a + 2 * stride + i);
-  const float4 b0 = __ldg(base.b + i), b1 = __ldg(base.b + stride + i),
-               b2 = __ldg(base.b + 2 * stride + i);
-  m.e[0][0] = cpair(a0.x, a0.y, b0.x, b0.y);
-  m.e[0][1] = cpair(a0.z, a0.w, b0.z, b0.w);
-  m.e[0][2] = cpair(a1.x, a1.y, b1.x, b1.y);
-  m.e[1][0] = cpair(a1.z, a1.w, b1.z, b1.w);
-  m.e[1][1] = cpair(a2.x, a2.y, b2.x, b2.y);
-  m.e[1][2] = cpair(a2.z, a2.w, b2.z, b2.w);
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    const float4 v = __ldg(base.p + e * stride + i);
+    m.e[e / 3][e % 3].re = f2(v.x, v.y);
+    m.e[e / 3][e % 3].im = f2(v.z, v.w);
+  }
 }
 
-// both copies' g at site i, row 2 rebuilt as conj(row0 x row1) (per lane as unpack12)
-__device__ __forceinline__ void load12(const GPairPtr& base, size_t stride, int i, Mat3<f2>& m) {
+// the pair at site i, row 2 rebuilt as conj(row0 x row1) (lane for lane as unpack12)
+__device__ __forceinline__ void load12(const P12& base, size_t stride, int i, Mat3<f2>& m) {
   load12_rows01(base, stride, i, m);
   row2_from_01(m);
 }
 
-// a link shared by both copies, broadcast to both lanes
-__device__ __forceinline__ void broadcast(const Mat3<float>& s, Mat3<f2>& m, int rows) {
+// rows 0,1 of the pair at site i; with keep_x / keep_y a lane keeps `old` (its copy has
+// stopped: its stored bits are written back unchanged)
+__device__ __forceinline__ void store12(const P12& base, size_t stride, int i, const Mat3<f2>& m,
+                                        const Mat3<f2>& old, bool keep_x, bool keep_y) {
 #pragma unroll
-  for (int r = 0; r < 3; r++) {
-    if (r >= rows) break;
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      m.e[r][c].re = f2(s.e[r][c].re);
-      m.e[r][c].im = f2(s.e[r][c].im);
-    }
+  for (int e = 0; e < 6; e++) {
+    const cplx<f2> a = m.e[e / 3][e % 3], o = old.e[e / 3][e % 3];
+    base.p[e * stride + i] = make_float4(keep_x ? o.re.v.x : a.re.v.x, keep_y ? o.re.v.y : a.re.v.y,
+                                         keep_x ? o.im.v.x : a.im.v.x, keep_y ? o.im.v.y : a.im.v.y);
   }
 }
 
-// rows 0,1 of both copies' new g, lane x to field a and lane y to field b
-__device__ __forceinline__ void store12(float4* a, float4* b, size_t stride, int i,
-                                        const Mat3<f2>& m) {
-  a[i] = make_float4(m.e[0][0].re.v.x, m.e[0][0].im.v.x, m.e[0][1].re.v.x, m.e[0][1].im.v.x);
-  a[stride + i] =
-      make_float4(m.e[0][2].re.v.x, m.e[0][2].im.v.x, m.e[1][0].re.v.x, m.e[1][0].im.v.x);
-  a[2 * stride + i] =
-      make_float4(m.e[1][1].re.v.x, m.e[1][1].im.v.x, m.e[1][2].re.v.x, m.e[1][2].im.v.x);
-  b[i] = make_float4(m.e[0][0].re.v.y, m.e[0][0].im.v.y, m.e[0][1].re.v.y, m.e[0][1].im.v.y);
-  b[stride + i] =
-      make_float4(m.e[0][2].re.v.y, m.e[0][2].im.v.y, m.e[1][0].re.v.y, m.e[1][0].im.v.y);
-  b[2 * stride + i] =
-      make_float4(m.e[1][1].re.v.y, m.e[1][1].im.v.y, m.e[1][2].re.v.y, m.e[1][2].im.v.y);
+// one lane of a pair field read as a scalar FP32 matrix (the per-copy measurement)
+struct LaneP12 {
+  const float4* p;
+  int lane;
+  __device__ __forceinline__ LaneP12 operator+(size_t off) const {
+    LaneP12 r;
+    r.p = p + off;
+    r.lane = lane;
+    return r;
+  }
+};
+__device__ __forceinline__ void load12_rows01(const LaneP12& base, size_t stride, int i,
+                                              Mat3<float>& m) {
+#pragma unroll
+  for (int e = 0; e < 6; e++) {
+    const float4 v = __ldg(base.p + e * stride + i);
+    m.e[e / 3][e % 3] = base.lane ? cmk(v.y, v.w) : cmk(v.x, v.z);
+  }
 }
 
 }  // namespace gfx
