@@ -108,13 +108,15 @@ class ThermParams(_c.Structure):
 class Tuning(_c.Structure):
     _fields_ = [("block", _c.c_int * 2), ("staging", _c.c_int * 2), ("link_reals64", _c.c_int),
                 ("link_reals32", _c.c_int), ("checkinterval", _c.c_int),
-                ("sweep_ms", _c.c_double * 2), ("check_ms", _c.c_double * 2)]
+                ("sweep_ms", _c.c_double * 2), ("check_ms", _c.c_double * 2),
+                ("wide_regs", _c.c_int)]
 
     def as_dict(self):
         return {"block": list(self.block), "staging": list(self.staging),
                 "link_reals64": self.link_reals64, "link_reals32": self.link_reals32,
                 "checkinterval": self.checkinterval,
-                "sweep_ms": list(self.sweep_ms), "check_ms": list(self.check_ms)}
+                "sweep_ms": list(self.sweep_ms), "check_ms": list(self.check_ms),
+                "wide_regs": self.wide_regs}
 
 
 def _sig(name, res, args):
@@ -295,10 +297,12 @@ class Context:
         return t.as_dict()
 
     def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0,
-                   link_reals32=0):
+                   link_reals32=0, wide_regs=1):
         """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first,
-        2 plain loads with the odd half-sweep's blocks in reverse order."""
+        2 plain loads with the odd half-sweep's blocks in reverse order.  wide_regs: the
+        FP32 half-sweep kernel with its full register set (1) or 64 registers (0)."""
         t = Tuning()
+        t.wide_regs = wide_regs
         t.block[0], t.block[1] = block
         t.staging[0], t.staging[1] = staging
         t.link_reals64 = link_reals64

@@ -224,7 +224,7 @@ void enqueue_sweep(gfx_ctx* ctx, int prec, int ndir, double omega) {
   void* G = prec == 0 ? ctx->G32 : prec == 2 ? ctx->Gdf : ctx->G64;
   for (int p = 0; p < 2; p++)
     launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, U, G, p, omega, ctx->or_block[prec],
-                        ctx->or_pf[prec], ctx->stream);
+                        ctx->or_pf[prec], ctx->stream, ctx->or_wide);
   ctx->launches += 2;
 }
 
@@ -260,7 +260,7 @@ void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int 
   }
   enqueue_sweeps(ctx, 0, ndir, omega, n - 1);
   launch_or_halfsweep(0, 12, ndir, ctx->L, ctx->U32, ctx->G32, 0, omega, ctx->or_block[0],
-                      ctx->or_pf[0], ctx->stream);
+                      ctx->or_pf[0], ctx->stream, ctx->or_wide);
   launch_or_halfsweep_measure(ndir, ctx->L, ctx->U32, ctx->G32, omega, ctx->or_pf[0] == 2,
                               ctx->partials, ctx->stream);
   launch_measure_even(ndir, ctx->L, ctx->U32, ctx->G32, ctx->partials, ctx->stream);
@@ -393,6 +393,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->block = 128;
   ctx->or_block[0] = ctx->or_block[1] = ctx->or_block[2] = 128;
   ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 2;  // odd half-sweeps in reverse order
+  ctx->or_wide = 1;
   ctx->fuse_check = 1;
   ctx->Udf = ctx->Gdf = nullptr;
   ctx->udf_valid = false;
@@ -681,7 +682,7 @@ gfx_status gfx_or_halfsweep(gfx_ctx* ctx, int parity, double omega, int gauge, i
   }
   launch_or_halfsweep(prec, lnr(ctx, prec), ndir, ctx->L, prec == 0 ? ctx->U32 : ctx->U64,
                       prec == 0 ? ctx->G32 : ctx->G64, parity, omega, ctx->or_block[prec],
-                      ctx->or_pf[prec], ctx->stream);
+                      ctx->or_pf[prec], ctx->stream, ctx->or_wide);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(ctx->stream));
   return GFX_OK;

@@ -26,6 +26,7 @@ struct gfx_ctx {
   size_t u32_bytes;
   int block;
   int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
+  int or_wide;      // FP32 half-sweep kernel with its full register set (1) or 64 (0)
   int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch, 2 plain
                     // with the odd half-sweep's blocks in reverse order (the default)
   int fuse_check;   // FP32 checks fused into the last odd half-sweep when possible (default 1)

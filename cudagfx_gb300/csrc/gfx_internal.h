@@ -67,8 +67,10 @@ struct Reduced {
 // prec == 0, FP64 12 or 18 reals when prec == 1
 // mode: 0 plain loads, 1 L2 bulk prefetch per block, 2 plain loads with the blocks of
 // parity 1 in reverse order
+// wide: the FP32 12-real kernel with its full register set instead of 64 registers
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
-                         int parity, double omega, int block, int mode, cudaStream_t s);
+                         int parity, double omega, int block, int mode, cudaStream_t s,
+                         int wide = 0);
 // measure: compute precision (0 float, 1 double), g storage (0 float, 1 double)
 void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
                     const void* G, double* partials, int block, cudaStream_t s);

@@ -44,8 +44,11 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // index order: after a half-sweep in forward order, the next one then starts on the
 // ranges the previous one touched last, which L2 may still hold.  The sites of one
 // parity are independent, so the order does not change the result.
-template <typename T, int NRU, int NDIR, int MODE>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) or_halfsweep_kernel(Lattice L,
+// WIDE = 0 caps an FP32 kernel at 64 registers (4 blocks of 256 per SM); WIDE = 1 leaves
+// it its full register set (~124), with which the compiler keeps more loads in flight
+// per warp (on GB300 7% faster on 32^4 at half the resident warps)
+template <typename T, int NRU, int NDIR, int MODE, int WIDE = 0>
+__global__ void __launch_bounds__(256, WIDE ? 1 : (sizeof(T) == 4 ? 4 : 2)) or_halfsweep_kernel(Lattice L,
                                                             const typename VecOf<T>::type* U,
                                                             typename VecOf<T>::type* G, int parity,
                                                             T omega, int rev) {
@@ -63,8 +66,23 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) or_halfsweep_kern
 }
 
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
-                         int parity, double omega, int block, int mode, cudaStream_t s) {
+                         int parity, double omega, int block, int mode, cudaStream_t s,
+                         int wide) {
   const dim3 grid((L.vh + block - 1) / block);
+  if (prec == 0 && link_nr == 12 && wide) {
+    const float4* u_ = (const float4*)U;
+    float4* g_ = (float4*)G;
+    const float w = (float)omega;
+    if (mode == 1) {
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 1, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, 0);
+      else or_halfsweep_kernel<float, 12, 3, 1, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, 0);
+    } else {
+      const int rev = mode == 2 ? parity : 0;
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 0, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, rev);
+      else or_halfsweep_kernel<float, 12, 3, 0, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, rev);
+    }
+    return;
+  }
 #define OR_LAUNCH(T, NR, ND)                                                                     \
   do {                                                                                           \
     const auto* u_ = (const typename VecOf<T>::type*)U;                                          \

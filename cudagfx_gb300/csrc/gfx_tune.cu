@@ -31,6 +31,7 @@ gfx_status gfx_get_tuning(const gfx_ctx* ctx, gfx_tuning* t) {
   t->link_reals64 = ctx->link_nr;
   t->link_reals32 = ctx->link_nr32;
   t->checkinterval = ctx->tune_ck;
+  t->wide_regs = ctx->or_wide;
   return GFX_OK;
 }
 
@@ -51,6 +52,8 @@ gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
   if (t->checkinterval < 0) return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: checkinterval < 0");
   if (t->link_reals32 != 0 && t->link_reals32 != 12 && t->link_reals32 != 8)
     return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals32 must be 0, 12 or 8");
+  if (t->wide_regs != 0 && t->wide_regs != 1)
+    return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: wide_regs must be 0 or 1");
   if (t->link_reals64) {
     gfx_status s = relayout_links(ctx, t->link_reals64);
     if (s) return s;
@@ -63,6 +66,7 @@ gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
     ctx->or_block[p] = t->block[p];
     ctx->or_pf[p] = t->staging[p];
   }
+  ctx->or_wide = t->wide_regs;
   ctx->tune_ck = t->checkinterval;
   destroy_graphs(ctx);
   return GFX_OK;
@@ -103,7 +107,7 @@ static std::string tune_key(const gfx_ctx* ctx, int ndir) {
 }
 
 // cache line: key TAB block0 staging0 block1 staging1 link_reals64 link_reals32 sweep_ms0
-// sweep_ms1 check_ms0 check_ms1
+// sweep_ms1 check_ms0 check_ms1 wide_regs
 static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t) {
   FILE* f = std::fopen(path, "r");
   if (!f) return false;
@@ -114,10 +118,10 @@ static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t
     if (!tab || std::string(line, tab - line) != key) continue;
     gfx_tuning c;
     std::memset(&c, 0, sizeof(c));
-    if (std::sscanf(tab + 1, "%d %d %d %d %d %d %lf %lf %lf %lf", &c.block[0], &c.staging[0],
+    if (std::sscanf(tab + 1, "%d %d %d %d %d %d %lf %lf %lf %lf %d", &c.block[0], &c.staging[0],
                     &c.block[1], &c.staging[1], &c.link_reals64, &c.link_reals32, &c.sweep_ms[0],
-                    &c.sweep_ms[1], &c.check_ms[0], &c.check_ms[1]) == 10 &&
-        (c.link_reals32 == 12 || c.link_reals32 == 8) &&
+                    &c.sweep_ms[1], &c.check_ms[0], &c.check_ms[1], &c.wide_regs) == 11 &&
+        (c.wide_regs == 0 || c.wide_regs == 1) && (c.link_reals32 == 12 || c.link_reals32 == 8) &&
         valid_block(c.block[0]) && valid_block(c.block[1]) &&
         (c.link_reals64 == 12 || c.link_reals64 == 18)) {
       *t = c;  // the last valid line for a key wins
@@ -131,9 +135,9 @@ static bool cache_lookup(const char* path, const std::string& key, gfx_tuning* t
 static void cache_append(const char* path, const std::string& key, const gfx_tuning& t) {
   FILE* f = std::fopen(path, "a");
   if (!f) return;  // the cache is an optimisation; an unwritable path only costs a re-tune
-  std::fprintf(f, "%s\t%d %d %d %d %d %d %.6g %.6g %.6g %.6g\n", key.c_str(), t.block[0],
+  std::fprintf(f, "%s\t%d %d %d %d %d %d %.6g %.6g %.6g %.6g %d\n", key.c_str(), t.block[0],
                t.staging[0], t.block[1], t.staging[1], t.link_reals64, t.link_reals32,
-               t.sweep_ms[0], t.sweep_ms[1], t.check_ms[0], t.check_ms[1]);
+               t.sweep_ms[0], t.sweep_ms[1], t.check_ms[0], t.check_ms[1], t.wide_regs);
   std::fclose(f);
 }
 
@@ -192,7 +196,7 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
       layouts[1] = 8;
     }
     double best = 1e30;
-    int bb = ctx->or_block[prec], bp = ctx->or_pf[prec], bnr = layouts[0];
+    int bb = ctx->or_block[prec], bp = ctx->or_pf[prec], bnr = layouts[0], bw = ctx->or_wide;
     int n = 0;
     for (int li = 0; li < nlayouts && s == GFX_OK; li++) {
       if (prec == 1 && (s = relayout_links(ctx, layouts[li]))) break;
@@ -206,25 +210,31 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
       }
       auto sweep = [&]() { enqueue_sweeps(ctx, prec, ndir, 1.7, n); };
       const int nmodes = 3;
+      // FP32 12-real sweeps: both register budgets of the kernel
+      const int nwide = prec == 0 && layouts[li] == 12 ? 2 : 1;
       for (int round = 0; round < 2 && s == GFX_OK; round++)
-        for (int bi = 0; bi < 4 && s == GFX_OK; bi++)
-          for (int pf = 0; pf < nmodes && s == GFX_OK; pf++) {
-            ctx->or_block[prec] = blocks[bi];
-            ctx->or_pf[prec] = pf;
-            double ms = 0.0;
-            s = time_reps(ctx, 2, sweep, &ms);
-            ms /= n;
-            if (s == GFX_OK && ms < best) {
-              best = ms;
-              bb = blocks[bi];
-              bp = pf;
-              bnr = layouts[li];
+        for (int w = 0; w < nwide && s == GFX_OK; w++)
+          for (int bi = 0; bi < 4 && s == GFX_OK; bi++)
+            for (int pf = 0; pf < nmodes && s == GFX_OK; pf++) {
+              ctx->or_block[prec] = blocks[bi];
+              ctx->or_pf[prec] = pf;
+              if (prec == 0) ctx->or_wide = nwide == 2 ? w : 0;
+              double ms = 0.0;
+              s = time_reps(ctx, 2, sweep, &ms);
+              ms /= n;
+              if (s == GFX_OK && ms < best) {
+                best = ms;
+                bb = blocks[bi];
+                bp = pf;
+                bnr = layouts[li];
+                if (prec == 0) bw = ctx->or_wide;
+              }
             }
-          }
     }
     if (s) break;
     ctx->or_block[prec] = bb;
     ctx->or_pf[prec] = bp;
+    if (prec == 0) ctx->or_wide = bw;
     if (prec == 1 && (s = relayout_links(ctx, bnr))) break;
     if (prec == 0 && (s = set_link_layout32(ctx, bnr))) break;
     ctx->tune_sweep_ms[prec] = best;

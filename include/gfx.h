@@ -178,6 +178,9 @@ typedef struct {
   int checkinterval;
   double sweep_ms[2];
   double check_ms[2];
+  int wide_regs; /* FP32 half-sweep kernel: 0 capped at 64 registers (32 warps per SM), 1
+                    its full register set (~124; 16 warps per SM, more loads in flight per
+                    warp); the results are bit-identical */
 } gfx_tuning;
 
 gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
@@ -186,7 +189,8 @@ gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
 gfx_status gfx_set_tuning(gfx_ctx *ctx, const gfx_tuning *t);
 /* Time every candidate setting on this context's lattice and apply the fastest.
  * Candidates: block 64/128/192/256 x staging 0/1/2 for each precision the
- * context holds, and both link layouts of each precision.  The fields are left as they
+ * context holds (x both register budgets for FP32), and both link layouts of each
+ * precision.  The fields are left as they
  * were: the candidate sweeps run on g and it is restored afterwards.
  * expected_sweeps > 0 also sets checkinterval to the interval that minimises
  * check time plus the sweeps run past convergence, sqrt(2 n check_ms / sweep_ms),

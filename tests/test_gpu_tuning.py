@@ -28,13 +28,15 @@ def test_launch_variants_are_bit_identical(prec):
     want = ref.get_trafo()
     ref.close()
     for nr in ((12, 18) if prec == 1 else (12,)):
-        for block in (32, 64, 96, 128, 192, 256):
-            for pf in (0, 1, 2):
-                c = _ctx()
-                c.set_tuning(block=(block, block), staging=(pf, pf), link_reals64=nr)
-                c.or_sweeps(3, omega=1.7, precision=prec)
-                assert np.array_equal(c.get_trafo(), want), (nr, block, pf)
-                c.close()
+        for wide in ((0, 1) if prec == 0 else (1,)):
+            for block in (32, 64, 96, 128, 192, 256):
+                for pf in (0, 1, 2):
+                    c = _ctx()
+                    c.set_tuning(block=(block, block), staging=(pf, pf), link_reals64=nr,
+                                 wide_regs=wide)
+                    c.or_sweeps(3, omega=1.7, precision=prec)
+                    assert np.array_equal(c.get_trafo(), want), (nr, wide, block, pf)
+                    c.close()
 
 
 def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
@@ -48,7 +50,7 @@ def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
     t = b.autotune(expected_sweeps=1000, cache_path=str(tmp_path / "tune.txt"))
     assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1, 2)
     assert t["link_reals64"] in (12, 18) and 5 <= t["checkinterval"] <= 100
-    assert t["link_reals32"] in (12, 8)
+    assert t["link_reals32"] in (12, 8) and t["wide_regs"] in (0, 1)
     assert t["sweep_ms"][0] > 0 and t["check_ms"][1] > 0
     assert np.array_equal(b.get_trafo(), g0)
     assert np.max(np.abs(b.get_links() - u0)) < 1e-15
