@@ -568,6 +568,7 @@ gfx_status gfx_set_links(gfx_ctx* ctx, const double* su3) {
     ctx->io_direct[0] = 1;
   }
   ctx->udf_valid = false;
+  ctx->rb_valid = false;  // the rebased links follow the FP64 links too
   // the FP32 12-real copy is written in the same pass (the 8-real one from U64 after)
   const bool with32 = ctx->U32 && ctx->link_nr32 == 12;
   launch_pack_links_tiled(ctx->link_nr, ctx->L, src, ctx->U64, with32 ? ctx->U32 : nullptr,
