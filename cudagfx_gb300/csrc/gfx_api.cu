@@ -252,27 +252,45 @@ void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
   ctx->launches += 1;
 }
 
-void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n) {
-  if (prec != 0 || n < 1 || !ctx->fuse_check || !fused_check_ok(ctx->L, ctx->link_nr32)) {
+bool odd_only_checks(const gfx_ctx* ctx, int prec) {
+  return prec == 0 && ctx->precision == GFX_PREC_MIXED && fused_check_ok(ctx->L, ctx->link_nr32);
+}
+
+// n sweeps, then the check's partials.  FP32 with fused_check_ok: the last odd
+// half-sweep writes the odd sites' partials (fuse_check) or a measurement of the odd
+// sites does; odd_only stops there, else the even sites are measured as well.
+void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n,
+                            bool odd_only) {
+  const bool ok = prec == 0 && n >= 1 && fused_check_ok(ctx->L, ctx->link_nr32);
+  if (!ok) {
     enqueue_sweeps(ctx, prec, ndir, omega, n);
     enqueue_measure(ctx, prec, prec, ndir);
     return;
   }
-  enqueue_sweeps(ctx, 0, ndir, omega, n - 1);
-  launch_or_halfsweep(0, 12, ndir, ctx->L, ctx->U32, ctx->G32, 0, omega, ctx->or_block[0],
-                      ctx->or_pf[0], ctx->stream, ctx->or_wide);
-  launch_or_halfsweep_measure(ndir, ctx->L, ctx->U32, ctx->G32, omega, ctx->or_pf[0] == 2,
-                              ctx->partials, ctx->stream);
-  launch_measure_even(ndir, ctx->L, ctx->U32, ctx->G32, ctx->partials, ctx->stream);
-  ctx->launches += 3;
+  if (ctx->fuse_check) {
+    enqueue_sweeps(ctx, 0, ndir, omega, n - 1);
+    launch_or_halfsweep(0, 12, ndir, ctx->L, ctx->U32, ctx->G32, 0, omega, ctx->or_block[0],
+                        ctx->or_pf[0], ctx->stream, ctx->or_wide);
+    launch_or_halfsweep_measure(ndir, ctx->L, ctx->U32, ctx->G32, omega, ctx->or_pf[0] == 2,
+                                ctx->partials, ctx->stream);
+    ctx->launches += 2;
+  } else {
+    enqueue_sweeps(ctx, 0, ndir, omega, n);
+    launch_measure_parity(ndir, ctx->L, ctx->U32, ctx->G32, ctx->partials, 1, ctx->stream);
+    ctx->launches += 1;
+  }
+  if (!odd_only) {
+    launch_measure_parity(ndir, ctx->L, ctx->U32, ctx->G32, ctx->partials, 0, ctx->stream);
+    ctx->launches += 1;
+  }
 }
 
 void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
-                           unsigned long long handle, int use_handle) {
+                           unsigned long long handle, int use_handle, bool odd_only) {
   const int nbx = measure_blocks_x(ctx->L, meas_block(ctx));
   launch_reduce(ctx->L, ndir, ctx->partials, nbx, ctx->slice_sums, ctx->reduced,
                 with_loop ? ctx->loop : nullptr, with_loop ? ctx->hist : nullptr, advance, handle,
-                use_handle, ctx->stream);
+                use_handle, ctx->stream, odd_only ? 1 : 0);
   ctx->launches += 2;
 }
 
@@ -786,15 +804,17 @@ void gfx_or_params_default(gfx_or_params* p) {
 // body of the device-side loop: ck sweeps, measurement, reduction + check
 static void enqueue_body(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
                          unsigned long long handle, int use_handle) {
-  enqueue_sweeps_measure(ctx, prec, ndir, omega, ck);
-  enqueue_reduce(ctx, ndir, true, ck, handle, use_handle);
+  const bool odd = odd_only_checks(ctx, prec);
+  enqueue_sweeps_measure(ctx, prec, ndir, omega, ck, odd);
+  enqueue_reduce(ctx, ndir, true, ck, handle, use_handle, odd);
 }
 
 static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
-                            cudaGraphExec_t* exec) {
+                            cudaGraphExec_t* exec, unsigned long long* body_out = nullptr) {
   for (auto& g : ctx->graphs)
     if (g.cprec == prec && g.ndir == ndir && g.ck == ck && g.omega == omega) {
       *exec = g.exec;
+      if (body_out) *body_out = g.body_launches;
       return GFX_OK;
     }
   cudaGraph_t graph;
@@ -810,7 +830,9 @@ static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double ome
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CK(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0,
                                    cudaStreamCaptureModeThreadLocal));
+  const unsigned long long l0 = ctx->launches;
   enqueue_body(ctx, prec, ndir, ck, omega, (unsigned long long)handle, 1);
+  const unsigned long long nbody = ctx->launches - l0;
   cudaGraph_t captured;
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &captured);
   if (e != cudaSuccess) {
@@ -827,7 +849,9 @@ static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double ome
   ge.omega = omega;
   ge.exec = ex;
   ge.graph = graph;
+  ge.body_launches = nbody;
   ctx->graphs.push_back(ge);
+  if (body_out) *body_out = nbody;
   *exec = ex;
   return GFX_OK;
 }
@@ -895,9 +919,12 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
 
   int sweeps_single = 0, sweeps_double = 0, sweeps_df = 0, sweeps_rb = 0;
   // iteration 0: sweep, then the first check (overrelax.cu:710-789)
-  enqueue_sweeps_measure(ctx, prec, ndir, p.omega, 1);
+  {
+    const bool odd = odd_only_checks(ctx, prec);
+    enqueue_sweeps_measure(ctx, prec, ndir, p.omega, 1, odd);
+    enqueue_reduce(ctx, ndir, true, 0, 0, 0, odd);
+  }
   (prec == 0 ? sweeps_single : sweeps_double)++;
-  enqueue_reduce(ctx, ndir, true, 0, 0, 0);
   CK(cudaGetLastError());
   s = read_loop(ctx);
   if (s) return s;
@@ -907,14 +934,15 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
       const int it0 = H.iter;
       if (p.use_graph) {
         cudaGraphExec_t ex = nullptr;
-        s = get_graph(ctx, prec, ndir, H.ck, p.omega, &ex);
-        if (s) return s;
+        unsigned long long nbody = 0;
         const unsigned long long before = ctx->launches;
+        s = get_graph(ctx, prec, ndir, H.ck, p.omega, &ex, &nbody);
+        if (s) return s;
         CK(cudaGraphLaunch(ex, ctx->stream));
         s = read_loop(ctx);
         if (s) return s;
-        // capture counted one body; add one body per executed iteration
-        ctx->launches = before + (unsigned long long)((H.iter - it0) / H.ck) * (2 * H.ck + 3);
+        // one body per executed iteration (a capture counts nothing that runs)
+        ctx->launches = before + (unsigned long long)((H.iter - it0) / H.ck) * nbody;
       } else {
         while (H.done == 0) {
           enqueue_body(ctx, prec, ndir, H.ck, p.omega, 0, 0);

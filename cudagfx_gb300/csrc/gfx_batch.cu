@@ -50,6 +50,8 @@ struct BConf {
   size_t part_base;  // first partial triple of copy 0 (copy k: + k * 2 * lt * nbx)
   int slice_base;    // first slice triple of copy 0 (copy k: + k * lt)
   int sitem_base;    // first slice-reduce item
+  int odd_only;      // FP32-phase checks measure the odd sites only, as a single
+                     // mixed solve of this lattice does (gfx_internal.h)
   int npairs;        // copy pairs (copies 2k, 2k+1; the last one alone when ncopies is odd)
   int pitem_base;    // first paired-sweep work item
 };
@@ -172,13 +174,14 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
   local -= parity * C.L.lt * C.nbx;
   const int t = local / C.nbx, bx = local - t * C.nbx;
   if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
+  if (F32 && C.odd_only && parity == 0) return;  // the FP32-phase checks: odd sites only
   typedef typename VecOf<TC>::type VU;
   typedef typename VecOf<TSG>::type VG;
   const VU* U = (const VU*)(sizeof(TC) == 4 ? C.U32 : C.U64);
   const VG* G = (const VG*)(sizeof(TSG) == 4 ? C.G32 : C.G64) +
                 (size_t)copy * (sizeof(TSG) == 4 ? C.gstride32 : C.gstride64);
   const int k = bx * blockDim.x + threadIdx.x;
-  constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
   double f = 0.0, dd = 0.0;
   float f32 = 0.0f, d32 = 0.0f;
   if (k < C.L.st) {
@@ -240,21 +243,27 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_rebased_kernel(BDes
   block_reduce3(f, dd, dd, out);
 }
 
-// per (copy, slice) sums, as slice_reduce_kernel
-__global__ void slice_batch_kernel(BDesc d) {
+// per (copy, slice) sums, as slice_reduce_kernel (f32check: an FP32 check, odd sites
+// only where the configuration's single solve does so)
+__global__ void slice_batch_kernel(BDesc d, int f32check) {
   const int ci = conf_of(d, blockIdx.x, &BConf::sitem_base);
   const BConf& C = d.c[ci];
   const int local = blockIdx.x - C.sitem_base;
   const int copy = local / C.L.lt, t = local - copy * C.L.lt;
   if (d.states[C.copy_base + copy].done != 0) return;
   const double* partials = d.partials + 3 * (C.part_base + (size_t)copy * 2 * C.L.lt * C.nbx);
+  const bool odd_only = f32check && C.odd_only;
   double f = 0.0, dd = 0.0, m = 0.0;
-  for (int j = threadIdx.x; j < 2 * C.nbx; j += blockDim.x) {
+  for (int j = (odd_only ? C.nbx : 0) + threadIdx.x; j < 2 * C.nbx; j += blockDim.x) {
     const int p = j / C.nbx, bx = j % C.nbx;
     const double* q = partials + 3 * ((size_t)(p * C.L.lt + t) * C.nbx + bx);
     f += q[0];
     dd += q[1];
     m = fmax(m, q[2]);
+  }
+  if (odd_only) {
+    f *= 2.0;
+    dd *= 2.0;
   }
   block_reduce3(f, dd, m, d.slice_sums + 3 * (C.slice_base + (size_t)copy * C.L.lt + t));
 }
@@ -450,7 +459,7 @@ void enqueue_check(gfx_batch* b, int cprec, int gprec, int ndir, int advance,
     if (ndir == 4) measure_batch_kernel<double, double, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
     else measure_batch_kernel<double, double, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
   }
-  slice_batch_kernel<<<b->nsitems, 256, 0, b->stream>>>(b->desc);
+  slice_batch_kernel<<<b->nsitems, 256, 0, b->stream>>>(b->desc, cprec == 0 && gprec == 0);
   check_batch_kernel<<<b->ncopies, 256, 0, b->stream>>>(b->desc, ndir, advance);
   continue_batch_kernel<<<1, 256, 0, b->stream>>>(b->desc, b->running,
                                                  (cudaGraphConditionalHandle)handle, use_handle);
@@ -645,6 +654,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     C.nblk = (C.L.vh + kBatchBlock - 1) / kBatchBlock;
     C.item_base = item;
     C.npairs = (C.ncopies + 1) / 2;
+    C.odd_only = precision == GFX_PREC_MIXED && fused_check_ok(C.L, 12) ? 1 : 0;
     C.pitem_base = pitem;
     C.nbx = (C.L.st + kBatchBlock - 1) / kBatchBlock;
     C.mitem_base = mitem;

@@ -75,6 +75,7 @@ struct gfx_ctx {
     double omega;
     cudaGraphExec_t exec;
     cudaGraph_t graph;
+    unsigned long long body_launches;  // kernels in one execution of the loop body
   };
   std::vector<GraphEntry> graphs;
   std::vector<gfx::CheckRecord> last_hist;
@@ -146,9 +147,12 @@ void enqueue_sweeps(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
 void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir);
 // n sweeps followed by the check's measurement (the same partials either way; FP32
 // with fused_check_ok: the last odd half-sweep writes the odd sites' partials)
-void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n);
+void enqueue_sweeps_measure(gfx_ctx* ctx, int prec, int ndir, double omega, int n,
+                            bool odd_only = false);
+// the FP32-phase checks of a mixed solve measure the odd sites only (gfx_internal.h)
+bool odd_only_checks(const gfx_ctx* ctx, int prec);
 void enqueue_reduce(gfx_ctx* ctx, int ndir, bool with_loop, int advance,
-                    unsigned long long handle, int use_handle);
+                    unsigned long long handle, int use_handle, bool odd_only = false);
 // re-pack the FP64 links as nr reals per link (12 or 18)
 gfx_status relayout_links(gfx_ctx* ctx, int nr);
 // FP32 link layout 12 or 8

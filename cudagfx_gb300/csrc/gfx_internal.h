@@ -80,15 +80,24 @@ constexpr int kMeasBlock = 128;
 // FP32 checks fused into the last odd half-sweep: possible for 12-real FP32 links when
 // every time slice holds whole measurement blocks of each parity
 bool fused_check_ok(const Lattice& L, int link_nr32);
+// The FP32-phase checks of a mixed-precision solve measure the odd sites only, which
+// the fused half-sweep has in registers.  Every link has exactly one odd end, so the
+// sum of Re tr X(x) over the odd sites covers each link once: doubled, it is the
+// all-site sum and F is exact.  tr[Delta Delta^+] summed over the odd sites and doubled
+// estimates the all-site dAdA (and theta); max dAdA is the odd sites' maximum.  These
+// checks only steer the FP32 phase (its plateau test and handover); convergence is
+// always decided by a full FP64 measurement.
 // the odd half-sweep that also writes the odd sites' partials (launch_measure's layout)
 void launch_or_halfsweep_measure(int ndir, const Lattice& L, const void* U, void* G, double omega,
                                  int rev, double* partials, cudaStream_t s);
-// launch_measure's FP32 even-site blocks only
-void launch_measure_even(int ndir, const Lattice& L, const void* U, const void* G,
-                         double* partials, cudaStream_t s);
+// launch_measure's FP32 blocks of one parity only
+void launch_measure_parity(int ndir, const Lattice& L, const void* U, const void* G,
+                           double* partials, int parity, cudaStream_t s);
+// odd_only: sum the odd sites' partials alone, F and dAdA doubled (FP32-phase checks)
 void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
                    Reduced* out, LoopState* loop, CheckRecord* hist, int advance,
-                   unsigned long long graph_handle, int use_handle, cudaStream_t s);
+                   unsigned long long graph_handle, int use_handle, cudaStream_t s,
+                   int odd_only = 0);
 void launch_plaquette(int link_nr_prec, const Lattice& L, const void* U, double* partials,
                       double* out, cudaStream_t s);
 void launch_polyakov(int link_nr_prec, const Lattice& L, const void* U, double* partials,

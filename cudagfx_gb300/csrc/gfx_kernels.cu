@@ -125,10 +125,11 @@ template <typename TC, typename TSU, int NRU, typename TSG, int NDIR>
 __global__ void __launch_bounds__(256) measure_kernel(Lattice L,
                                                        const typename VecOf<TSU>::type* U,
                                                        const typename VecOf<TSG>::type* G,
-                                                       double* partials) {
+                                                       double* partials, int parity0) {
   // parity is the inner grid dimension: both parities of a slice run back to back, so
-  // the links and g they share are read from L2 the second time
-  const int parity = blockIdx.y, t = blockIdx.z;
+  // the links and g they share are read from L2 the second time (a grid of one parity
+  // measures parity0 only)
+  const int parity = parity0 + blockIdx.y, t = blockIdx.z;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
   double f = 0.0, d = 0.0;
@@ -201,16 +202,16 @@ void launch_or_halfsweep_measure(int ndir, const Lattice& L, const void* U, void
         L, (const float4*)U, (float4*)G, (float)omega, rev, nbx, partials);
 }
 
-// the measurement's even-site blocks only (the odd ones come from the fused sweep)
-void launch_measure_even(int ndir, const Lattice& L, const void* U, const void* G,
-                         double* partials, cudaStream_t s) {
+// the FP32 measurement's blocks of one parity only
+void launch_measure_parity(int ndir, const Lattice& L, const void* U, const void* G,
+                           double* partials, int parity, cudaStream_t s) {
   const dim3 grid(measure_blocks_x(L, kMeasBlock), 1, L.lt);
   if (ndir == 4)
     measure_kernel<float, float, 12, float, 4><<<grid, kMeasBlock, 0, s>>>(
-        L, (const float4*)U, (const float4*)G, partials);
+        L, (const float4*)U, (const float4*)G, partials, parity);
   else
     measure_kernel<float, float, 12, float, 3><<<grid, kMeasBlock, 0, s>>>(
-        L, (const float4*)U, (const float4*)G, partials);
+        L, (const float4*)U, (const float4*)G, partials, parity);
 }
 
 int measure_blocks_x(const Lattice& L, int block) { return (L.st + block - 1) / block; }
@@ -221,7 +222,7 @@ void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& 
 #define MEAS(TC, TSU, NR, TSG, ND)                                                    \
   measure_kernel<TC, TSU, NR, TSG, ND><<<grid, block, 0, s>>>(                      \
       L, (const typename VecOf<TSU>::type*)U, (const typename VecOf<TSG>::type*)G, \
-      partials)
+      partials, 0)
   if (cprec == 2) {  // double-float, 18-real links, double-float g
     if (ndir == 4) MEAS(dfl, dfl, 18, dfl, 4);
     else MEAS(dfl, dfl, 18, dfl, 3);
@@ -251,16 +252,24 @@ void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& 
 #undef MEAS
 }
 
-// per-slice sums: block t reduces both parities' partials of slice t (fixed order)
-__global__ void slice_reduce_kernel(const double* partials, int nbx, int lt, double* slice_sums) {
+// per-slice sums: block t reduces both parities' partials of slice t (fixed order).
+// odd_only: the odd sites' partials alone, their F and dAdA sums doubled (the FP32-phase
+// checks, gfx_internal.h)
+__global__ void slice_reduce_kernel(const double* partials, int nbx, int lt, double* slice_sums,
+                                    int odd_only) {
   const int t = blockIdx.x;
   double f = 0.0, d = 0.0, m = 0.0;
-  for (int j = threadIdx.x; j < 2 * nbx; j += blockDim.x) {
+  const int j0 = odd_only ? nbx : 0;
+  for (int j = j0 + threadIdx.x; j < 2 * nbx; j += blockDim.x) {
     const int p = j / nbx, bx = j % nbx;
     const double* q = partials + 3 * ((size_t)(p * lt + t) * nbx + bx);
     f += q[0];
     d += q[1];
     m = fmax(m, q[2]);
+  }
+  if (odd_only) {
+    f *= 2.0;
+    d *= 2.0;
   }
   block_reduce3(f, d, m, slice_sums + 3 * t);
 }
@@ -276,8 +285,8 @@ __global__ void final_reduce_kernel(const double* slice_sums, int lt, double vol
 
 void launch_reduce(const Lattice& L, int ndir, const double* partials, int nbx, double* slice_sums,
                    Reduced* out, LoopState* loop, CheckRecord* hist, int advance,
-                   unsigned long long graph_handle, int use_handle, cudaStream_t s) {
-  slice_reduce_kernel<<<L.lt, 256, 0, s>>>(partials, nbx, L.lt, slice_sums);
+                   unsigned long long graph_handle, int use_handle, cudaStream_t s, int odd_only) {
+  slice_reduce_kernel<<<L.lt, 256, 0, s>>>(partials, nbx, L.lt, slice_sums, odd_only);
   const double vol = 2.0 * (double)L.vh;
   const double v3 = (double)L.lx * L.ly * L.lz;
   final_reduce_kernel<<<1, 256, 0, s>>>(slice_sums, L.lt, vol, v3, ndir, out, loop, hist,

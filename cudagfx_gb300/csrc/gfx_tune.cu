@@ -241,9 +241,10 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
     if ((s = prepare_g(ctx, prec))) break;
     // the check's cost: a sweep with its check (fused when the loop fuses it) minus
     // a plain sweep
+    const bool odd = odd_only_checks(ctx, prec);
     auto check = [&]() {
-      enqueue_sweeps_measure(ctx, prec, ndir, 1.7, 1);
-      enqueue_reduce(ctx, ndir, false, 0, 0, 0);
+      enqueue_sweeps_measure(ctx, prec, ndir, 1.7, 1, odd);
+      enqueue_reduce(ctx, ndir, false, 0, 0, 0, odd);
     };
     s = time_reps(ctx, std::max(2, n), check, &ctx->tune_measure_ms[prec]);
     ctx->tune_measure_ms[prec] = std::max(0.0, ctx->tune_measure_ms[prec] - best);
