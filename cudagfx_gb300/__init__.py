@@ -79,7 +79,7 @@ class ORParams(_c.Structure):
                 ("switch_eps", _c.c_double), ("plateau_ratio", _c.c_double),
                 ("checkinterval_double", _c.c_int), ("use_graph", _c.c_int),
                 ("record_history", _c.c_int), ("checkinterval_near", _c.c_int),
-                ("polish", _c.c_int)]
+                ("polish", _c.c_int), ("fp32_checks_all_sites", _c.c_int)]
 
 
 class ORResult(_c.Structure):

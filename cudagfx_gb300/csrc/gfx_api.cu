@@ -253,7 +253,8 @@ void enqueue_measure(gfx_ctx* ctx, int cprec, int gprec, int ndir) {
 }
 
 bool odd_only_checks(const gfx_ctx* ctx, int prec) {
-  return prec == 0 && ctx->precision == GFX_PREC_MIXED && fused_check_ok(ctx->L, ctx->link_nr32);
+  return ctx->odd_checks && prec == 0 && ctx->precision == GFX_PREC_MIXED &&
+         fused_check_ok(ctx->L, ctx->link_nr32);
 }
 
 // n sweeps, then the check's partials.  FP32 with fused_check_ok: the last odd
@@ -413,6 +414,7 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
   ctx->or_pf[0] = ctx->or_pf[1] = ctx->or_pf[2] = 2;  // odd half-sweeps in reverse order
   ctx->or_wide = 1;
   ctx->fuse_check = 1;
+  ctx->odd_checks = 1;
   ctx->Udf = ctx->Gdf = nullptr;
   ctx->udf_valid = false;
   ctx->Ur = ctx->W0 = nullptr;
@@ -811,8 +813,9 @@ static void enqueue_body(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
 
 static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double omega,
                             cudaGraphExec_t* exec, unsigned long long* body_out = nullptr) {
+  const int odd = odd_only_checks(ctx, prec) ? 1 : 0;
   for (auto& g : ctx->graphs)
-    if (g.cprec == prec && g.ndir == ndir && g.ck == ck && g.omega == omega) {
+    if (g.cprec == prec && g.ndir == ndir && g.ck == ck && g.omega == omega && g.odd == odd) {
       *exec = g.exec;
       if (body_out) *body_out = g.body_launches;
       return GFX_OK;
@@ -850,6 +853,7 @@ static gfx_status get_graph(gfx_ctx* ctx, int prec, int ndir, int ck, double ome
   ge.exec = ex;
   ge.graph = graph;
   ge.body_launches = nbody;
+  ge.odd = odd;
   ctx->graphs.push_back(ge);
   if (body_out) *body_out = nbody;
   *exec = ex;
@@ -885,6 +889,7 @@ gfx_status gfx_overrelax(gfx_ctx* ctx, const gfx_or_params* pin, gfx_or_result* 
   if (s) return s;
   if (p.checkinterval_near < 0) return fail(ctx, GFX_ERR_ARG, "checkinterval_near must be >= 0");
   if (p.polish < 0 || p.polish > 2) return fail(ctx, GFX_ERR_ARG, "polish must be 0, 1 or 2");
+  ctx->odd_checks = p.fp32_checks_all_sites ? 0 : 1;
   const int ck_min = std::min(std::min(p.checkinterval, p.checkinterval_double),
                               p.checkinterval_near > 0 ? p.checkinterval_near : p.checkinterval);
   const int hist_need = p.maxit / ck_min + 8;

@@ -654,7 +654,7 @@ gfx_status gfx_batch_create(gfx_batch** out, int nconf, const int* dims, const i
     C.nblk = (C.L.vh + kBatchBlock - 1) / kBatchBlock;
     C.item_base = item;
     C.npairs = (C.ncopies + 1) / 2;
-    C.odd_only = precision == GFX_PREC_MIXED && fused_check_ok(C.L, 12) ? 1 : 0;
+    C.odd_only = 0;  // set per solve (gfx_batch_overrelax)
     C.pitem_base = pitem;
     C.nbx = (C.L.st + kBatchBlock - 1) / kBatchBlock;
     C.mitem_base = mitem;
@@ -833,6 +833,22 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
     H.eps = p.eps;
     H.switch_eps = p.switch_eps;
     H.plateau_ratio = p.plateau_ratio > 0 ? std::pow(p.plateau_ratio, p.checkinterval) : 1e300;
+  }
+  // the FP32-phase checks measure what a single mixed solve of each lattice measures
+  bool odd_changed = false;
+  for (int c = 0; c < b->nconf; c++) {
+    BConf& C = b->desc.c[c];
+    const int odd = handover && !p.fp32_checks_all_sites && fused_check_ok(C.L, 12) ? 1 : 0;
+    odd_changed |= odd != C.odd_only;
+    C.odd_only = odd;
+  }
+  if (odd_changed) {  // graphs captured the descriptor by value
+    BCK(cudaStreamSynchronize(b->stream));
+    for (auto& g : b->graphs) {
+      cudaGraphExecDestroy(g.exec);
+      cudaGraphDestroy(g.graph);
+    }
+    b->graphs.clear();
   }
   gfx_status s = write_states(b);
   if (s) return s;

@@ -30,6 +30,8 @@ struct gfx_ctx {
   int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch, 2 plain
                     // with the odd half-sweep's blocks in reverse order (the default)
   int fuse_check;   // FP32 checks fused into the last odd half-sweep when possible (default 1)
+  int odd_checks;   // the FP32-phase checks of a mixed solve may measure the odd sites only
+                    // (gfx_or_params.fp32_checks_all_sites = 0); set per gfx_overrelax
   double tune_sweep_ms[2], tune_measure_ms[2];
   int tune_ck;
   cudaStream_t stream;
@@ -76,6 +78,7 @@ struct gfx_ctx {
     cudaGraphExec_t exec;
     cudaGraph_t graph;
     unsigned long long body_launches;  // kernels in one execution of the loop body
+    int odd;                           // captured with odd-site FP32 checks
   };
   std::vector<GraphEntry> graphs;
   std::vector<gfx::CheckRecord> last_hist;

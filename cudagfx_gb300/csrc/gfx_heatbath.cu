@@ -6,6 +6,7 @@
 //     (heatbath_thermalization.cu:235-550), storing the result at link (x, nu).
 // Random numbers are read from the Mersenne-Twister fields with the reference's
 // indexing: gauss[k], unif[4k..4k+3] with k = eo index (SA) or 4*eo + nu (links).
+#include "gfx_common.cuh"
 #include "gfx_internal.h"
 
 namespace gfx {
@@ -169,12 +170,17 @@ __device__ __forceinline__ Su2<float> heatbath_su2_kp_f32(const Su2<float>& w, d
   return al;
 }
 
-// star for the gauge-transformation update (same as the OR kernel)
+// star for the gauge-transformation update (same as the OR kernel; FP32 with 12-real
+// links in the OR sweep's reduced form)
 template <typename T, int NRU, int NDIR>
 __device__ __forceinline__ void g_star(const Lattice& L, const Site& c, int parity,
                                        const typename VecOf<T>::type* __restrict__ U,
                                        const typename VecOf<T>::type* __restrict__ G,
                                        Mat3<T>& star) {
+  if constexpr (sizeof(T) == 4 && NRU == 12) {
+    compute_star_f32<NDIR>(L, c, parity, U, G, star);
+    return;
+  }
   constexpr int NCU = Field<T, NRU>::NCHUNK;
   constexpr int NCG = Field<T, 12>::NCHUNK;
   const size_t vh = (size_t)L.vh;
@@ -351,10 +357,12 @@ __global__ void __launch_bounds__(128) link_heatbath_kernel(Lattice L, double2* 
 
 // The same update in FP32 arithmetic, for thermalization: staples from the FP32 link
 // copy (12 reals), the SU(2) heatbath steps on an FP32 copy of the link, then the new
-// link is reunitarized in FP64 and stored in both copies, so they stay in step.  A
-// heatbath draws the new link at random; FP32 arithmetic moves the drawn link by
-// ~1e-7, far below the spread of the draw, so the chain samples the same
-// distribution, while the kernel runs on the FP32 units instead of the FP64 pipe.
+// link is reunitarized in double-float arithmetic (~48 bits, about 1e-14 from
+// unitary), widened to FP64 and stored in both copies (the FP32 one as the rounding of
+// the FP64 one), so they stay in step.  A heatbath draws the new link at random; FP32
+// arithmetic moves the drawn link by ~1e-7, far below the spread of the draw, so the
+// chain samples the same distribution, while the kernel runs on the FP32 units
+// instead of the FP64 pipe.
 __device__ __forceinline__ void ld_link32(const Lattice& L, const float4* __restrict__ U32,
                                           Coord c, int mu, Mat3<float>& m) {
   const int p = (c.x + c.y + c.z + c.t) & 1;
@@ -409,12 +417,21 @@ __global__ void __launch_bounds__(128) link_heatbath_f32_kernel(Lattice L, doubl
       su2_rotate(link, a, b, heatbath_su2_kp_f32(w, beta3, __ldg(gauss + r), __ldg(unif4 + r)));
     }
   }
-  Mat3<double> ld;
+  // Reunitarize in double-float (~48 bits, on the FP32 units; FP64 Gram-Schmidt made
+  // this kernel FP64-pipe bound on GB300) and widen: the FP64 link is unitary to ~1e-14
+  Mat3<dfl> lf;
 #pragma unroll
   for (int r = 0; r < 2; r++)
 #pragma unroll
-    for (int c = 0; c < 3; c++) ld.e[r][c] = cmk<double>(link.e[r][c].re, link.e[r][c].im);
-  normalize<double, true>(ld);
+    for (int c = 0; c < 3; c++)
+      lf.e[r][c] = cmk<dfl>(dfl(link.e[r][c].re, 0.0f), dfl(link.e[r][c].im, 0.0f));
+  normalize<dfl, NR == 18>(lf);
+  Mat3<double> ld;
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+      ld.e[r][c] = cmk<double>((double)lf.e[r][c].re, (double)lf.e[r][c].im);
   constexpr int NC = Field<double, NR>::NCHUNK;
   Field<double, NR>::store(U + (size_t)(parity * 4 + nu) * NC * L.vh, (size_t)L.vh, i, ld);
 #pragma unroll

@@ -82,6 +82,11 @@ typedef struct {
                              to ~1e-12 at FP32 cost.  The result of 1 and 2 is confirmed
                              by an FP64 measurement (FP64 sweeps continue if it is not).
                              GB300 runs FP32 64x faster than FP64. */
+  int fp32_checks_all_sites; /* mixed: 0 (default) = the FP32-phase checks measure the odd
+                                sites only when the check is fused into the last odd
+                                half-sweep (F exact, dAdA and theta estimated as twice the
+                                odd sites' sums); 1 = every site.  They only steer the FP32
+                                phase; convergence is decided by an FP64 measurement. */
 } gfx_or_params;
 
 typedef struct {

@@ -2,7 +2,8 @@
 thermalization (gfx_therm_params.precision = 1).  With the same random fields they
 follow their FP64 counterparts to FP32 rounding, except at accept/reject decisions
 that sit at the rounding boundary, and the FP32 thermalization samples the Wilson
-action: the beta = 6.0 plaquette, links in SU(3) to FP64 precision."""
+action: the beta = 6.0 plaquette, links in SU(3) to ~1e-14 (the new link is
+reunitarized in double-float arithmetic)."""
 import numpy as np
 import pytest
 
