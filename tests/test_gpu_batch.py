@@ -77,3 +77,36 @@ def test_paired_sweeps_bit_identical_to_one_copy_per_thread(gfx, ncopies):
     assert [r["F"] for r in rp] == [r["F"] for r in r1]
     for a, b in zip(gp, g1):
         assert np.array_equal(a, b)
+
+
+def test_batch_at_c4_sizes_matches_single_solves(gfx):
+    # the C4 lattices themselves (16^4 and 24^4, whose slices hold whole 128-site blocks,
+    # so the FP32-phase checks read the odd sites), a few copies each, with Kennedy-
+    # Pendleton-like rough links: every copy as its single mixed solve (the same checks,
+    # the same sweep split, g to 1e-12)
+    dims = [(16, 16, 16, 16), (24, 24, 24, 24)]
+    ncopies = [3, 2]
+    b = gfx.Batch(dims, ncopies, precision=gfx.PREC_MIXED)
+    links = [smooth_links(d, 0.9, 70 + c) for c, d in enumerate(dims)]
+    for c, u in enumerate(links):
+        b.set_links(c, u)
+    b.random_haar(4000)
+    kw = dict(maxit=6000, eps=1e-12, checkinterval=25, omega=1.7, criterion=gfx.CRIT_THETA,
+              polish=2)
+    res, _ = b.overrelax(**kw)
+    assert all(r["converged"] for r in res)
+    base = 0
+    for c, d in enumerate(dims):
+        ctx = gfx.Context(d, precision=gfx.PREC_MIXED)
+        ctx.set_links(links[c])
+        for k in range(ncopies[c]):
+            ctx.random_trafo_haar(4000 + base + k)
+            r = ctx.overrelax(**kw)
+            got = res[base + k]
+            assert (got["iterations"], got["sweeps_single"], got["sweeps_double"]) == \
+                (r.iterations, r.sweeps_single, r.sweeps_double)
+            assert got["F"] == pytest.approx(r.final_values.F, rel=1e-13)
+            assert got["theta"] == pytest.approx(r.final_values.theta, rel=1e-9)
+            assert np.max(np.abs(b.get_trafo(c, k) - ctx.get_trafo())) < 1e-12
+        ctx.close()
+        base += ncopies[c]
