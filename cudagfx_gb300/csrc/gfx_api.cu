@@ -1431,7 +1431,8 @@ unsigned long long gfx_launch_count(const gfx_ctx* ctx) { return ctx ? ctx->laun
 
 void* gfx_host_alloc(size_t bytes) {
   void* p = nullptr;
-  if (cudaMallocHost(&p, bytes) != cudaSuccess) {
+  // portable and mapped: every context of the process may read and write it directly
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }

@@ -79,22 +79,36 @@ def test_paired_sweeps_bit_identical_to_one_copy_per_thread(gfx, ncopies):
         assert np.array_equal(a, b)
 
 
-def test_batch_at_c4_sizes_matches_single_solves(gfx):
+def _heatbath_links(gfx, dims, beta, sweeps, seed, mt_params):
+    V = int(np.prod(dims))
+    c = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    c.set_links(gfx.unit_init(4 * V))
+    c.mt_load_params(mt_params)
+    c.mt_seed(seed)
+    c.mt_init(2 * V, 8 * V)
+    c.thermalize(beta, sweeps, variant=gfx.HB_KENNEDY_PENDLETON)
+    u = c.get_links()
+    c.close()
+    return u
+
+
+def test_batch_at_c4_sizes_matches_single_solves(gfx, mt_params):
     # the C4 lattices themselves (16^4 and 24^4, whose slices hold whole 128-site blocks,
-    # so the FP32-phase checks read the odd sites), a few copies each, with Kennedy-
-    # Pendleton-like rough links: every copy as its single mixed solve (the same checks,
-    # the same sweep split, g to 1e-12)
+    # so the FP32-phase checks read the odd sites), a few copies each, on Kennedy-
+    # Pendleton heatbath links at beta 6.0 / 6.2: every copy as its single mixed solve
+    # (the same checks, the same sweep split, g to 1e-12)
     dims = [(16, 16, 16, 16), (24, 24, 24, 24)]
     ncopies = [3, 2]
     b = gfx.Batch(dims, ncopies, precision=gfx.PREC_MIXED)
-    links = [smooth_links(d, 0.9, 70 + c) for c, d in enumerate(dims)]
+    links = [_heatbath_links(gfx, d, beta, 40, 70 + c, mt_params)
+             for c, (d, beta) in enumerate(zip(dims, (6.0, 6.2)))]
     for c, u in enumerate(links):
         b.set_links(c, u)
     b.random_haar(4000)
-    kw = dict(maxit=6000, eps=1e-12, checkinterval=25, omega=1.7, criterion=gfx.CRIT_THETA,
+    kw = dict(maxit=10000, eps=1e-12, checkinterval=25, omega=1.7, criterion=gfx.CRIT_THETA,
               polish=2)
     res, _ = b.overrelax(**kw)
-    assert all(r["converged"] for r in res)
+    assert all(r["converged"] for r in res), [(r["iterations"], r["theta"]) for r in res]
     base = 0
     for c, d in enumerate(dims):
         ctx = gfx.Context(d, precision=gfx.PREC_MIXED)
