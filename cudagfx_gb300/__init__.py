@@ -471,7 +471,8 @@ class Context:
 
     def thermalize(self, beta, nsweep, checkint=0, variant=HB_REFERENCE, precision=0):
         """precision 0: FP64 heatbath (the reference's arithmetic); 1: FP32 staples and
-        SU(2) steps with FP64 reunitarization (SINGLE or MIXED contexts)."""
+        SU(2) steps, reunitarized in double-float and stored in FP64 and FP32 (SINGLE or
+        MIXED contexts)."""
         p = ThermParams(nsweep, checkint, beta, variant, precision)
         cap = (nsweep + checkint - 1) // checkint if checkint > 0 else 0
         plaq = np.zeros(max(cap, 1))
