@@ -41,9 +41,10 @@ BYTES_PER_UPDATE_FP32 = 132 * 4
 BYTES_PER_UPDATE_FP64 = 132 * 8
 FLOP_PER_UPDATE = 4766  # the reference's count (overrelax.cu:897)
 # DRAM bytes per FP32 half-sweep launch at 32^4 (dram__bytes_read.sum +
-# dram__bytes_write.sum) in the alternating sweep with warm L2 (staging 2), from the
-# --cache-control none capture in profiles/or_halfsweep_fp32_32x4.md
-NCU_TRAFFIC_FP32 = {(32, 32, 32, 32): 198.4e6 + 27.2e6}
+# dram__bytes_write.sum) in the alternating sweep with warm L2, per staging mode, from
+# the --cache-control none captures in profiles/or_halfsweep_fp32_32x4.md
+NCU_TRAFFIC_FP32 = {((32, 32, 32, 32), 2): 198.4e6 + 27.2e6,
+                    ((32, 32, 32, 32), 4): 185.3e6 + 6.7e6}
 
 
 POLISH_NAMES = {0: "FP64", 1: "double-float (FP32 pairs), FP64-confirmed",
@@ -86,7 +87,7 @@ def parse():
                          "(--no-fp64 skips that solve): c1 8^4 (also on the CPU oracle), c2 "
                          "16^3x32 SA then OR, c3 32^4 Coulomb, c4 the batched Gribov copies "
                          "alone, c5 48^3x96")
-    ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2],
+    ap.add_argument("--staging", type=int, default=2, choices=[0, 1, 2, 3, 4],
                     help="--kernels: OR half-sweep staging mode")
     ap.add_argument("--kernels", action="store_true",
                     help="no timing: a few launches of each hot kernel on the lattice, for "
@@ -638,10 +639,11 @@ def run_gfx(args, dims):
     t64_share = r_last.sweeps_double * 2 * (ms64 if ms64 else 0.0)
     bytes32 = BYTES_PER_UPDATE_FP32 * V / 2
     ach32 = bytes32 / (ms32 / 1000.0) / 1e9
+    staging32 = ctx.tuning()["staging"][0]
     roof = {"bound": "hbm", "kernel": "or_halfsweep_kernel<float,12,4>",
             "achieved": ach32, "peak": hbm, "unit": "GB/s", "frac": ach32 / hbm,
-            "peak_source": peak_kind,
-            "traffic": NCU_TRAFFIC_FP32.get(tuple(dims)), "ms_per_launch": ms32,
+            "peak_source": peak_kind, "staging": staging32,
+            "traffic": NCU_TRAFFIC_FP32.get((tuple(dims), staging32)), "ms_per_launch": ms32,
             "bytes_per_launch": bytes32,
             "time_share_in_solve": t32_share / max(r_last.ms, 1e-9)}
     if ms64:

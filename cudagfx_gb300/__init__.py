@@ -299,7 +299,8 @@ class Context:
     def set_tuning(self, block=(128, 128), staging=(0, 0), link_reals64=0, checkinterval=0,
                    link_reals32=0, wide_regs=1):
         """staging per precision: 0 plain loads, 1 an L2 bulk prefetch per block first,
-        2 plain loads with the odd half-sweep's blocks in reverse order.  wide_regs: the
+        2 plain loads with the odd half-sweep's blocks in reverse order, 3 as 2 with the
+        FP32 g kept in L2 (evict_last), 4 as 3 with the FP32 links evict_first.  wide_regs: the
         FP32 half-sweep kernel with its full register set (1) or 64 registers (0)."""
         t = Tuning()
         t.wide_regs = wide_regs

@@ -166,6 +166,61 @@ __device__ __forceinline__ void acc_cross(cplx<T>& acc, cplx<T> p, cplx<T> q, cp
   acc.im = fm(p.re, q.im, fm(p.im, q.re, fm(-r.re, s.im, fm(-r.im, s.re, acc.im))));
 }
 
+// An FP32 12-real field read (and written) with an L2 eviction priority: pol is a
+// createpolicy handle, evict_last for g (48 MB for 32^4, so it can stay resident in
+// L2 while the 192 MB of links stream past it), evict_first for links.
+struct HintP {
+  const float4* p;
+  uint64_t pol;
+  __device__ __forceinline__ HintP operator+(size_t off) const { return {p + off, pol}; }
+};
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t pol;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+  return pol;
+}
+__device__ __forceinline__ float4 ldg_hint(const float4* p, uint64_t pol) {
+  float4 v;
+  asm("ld.global.nc.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ void stg_hint(float4* p, float4 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v4.f32 [%0], {%1, %2, %3, %4}, %5;" ::"l"(p), "f"(v.x),
+               "f"(v.y), "f"(v.z), "f"(v.w), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void load12_rows01(const HintP& base, size_t stride, int i,
+                                              Mat3<float>& m) {
+  const float4 a = ldg_hint(base.p + i, base.pol), b = ldg_hint(base.p + stride + i, base.pol),
+               c = ldg_hint(base.p + 2 * stride + i, base.pol);
+  m.e[0][0] = cmk(a.x, a.y);
+  m.e[0][1] = cmk(a.z, a.w);
+  m.e[0][2] = cmk(b.x, b.y);
+  m.e[1][0] = cmk(b.z, b.w);
+  m.e[1][1] = cmk(c.x, c.y);
+  m.e[1][2] = cmk(c.z, c.w);
+}
+__device__ __forceinline__ void load12_hint(const HintP& base, size_t stride, int i,
+                                            Mat3<float>& m) {
+  unpack12(ldg_hint(base.p + i, base.pol), ldg_hint(base.p + stride + i, base.pol),
+           ldg_hint(base.p + 2 * stride + i, base.pol), m);
+}
+__device__ __forceinline__ void store12_hint(float4* base, size_t stride, int i,
+                                             const Mat3<float>& m, uint64_t pol) {
+  stg_hint(base + i, make_float4(m.e[0][0].re, m.e[0][0].im, m.e[0][1].re, m.e[0][1].im), pol);
+  stg_hint(base + stride + i,
+           make_float4(m.e[0][2].re, m.e[0][2].im, m.e[1][0].re, m.e[1][0].im), pol);
+  stg_hint(base + 2 * stride + i,
+           make_float4(m.e[1][1].re, m.e[1][1].im, m.e[1][2].re, m.e[1][2].im), pol);
+}
+
 // loads of the FP32 star.  Scalar: one copy, 3 planes of float4 per matrix.  Pairs
 // (T = f2, gfx_pair.cuh): the P12 layout, 6 planes per matrix, for the two copies' g
 // and for the links held in both lanes; LaneP12 reads one copy of a pair field.
@@ -197,6 +252,17 @@ __device__ __forceinline__ void link_full(const P12& base, size_t stride, int i,
 }
 __device__ __forceinline__ void g_full(const P12& base, size_t stride, int i, Mat3<f2>& m) {
   load12(base, stride, i, m);
+}
+__device__ __forceinline__ void link_rows01(const HintP& base, size_t stride, int i,
+                                            Mat3<float>& m) {
+  load12_rows01(base, stride, i, m);
+}
+__device__ __forceinline__ void link_full(const HintP& base, size_t stride, int i,
+                                          Mat3<float>& m) {
+  load12_hint(base, stride, i, m);
+}
+__device__ __forceinline__ void g_full(const HintP& base, size_t stride, int i, Mat3<float>& m) {
+  load12_hint(base, stride, i, m);
 }
 template <typename P>
 struct Planes {
@@ -297,6 +363,29 @@ __device__ __forceinline__ void or_site_update(const Lattice& L, const Site& c, 
     overrelax_rows01(gn, gold, g, omega);
   }
   Field<T, 12>::store(Gp, vh, i, gn);
+}
+
+// The FP32 12-real update with L2 eviction priorities (staging modes 3 and 4): g read
+// and written as evict_last, so the 48 MB of a 32^4 g can stay in L2 while the links
+// stream; the links as evict_first (LINKS_FIRST) or with the default priority.  The
+// operations are those of or_site_update<float, 12, NDIR>.
+template <int NDIR, bool LINKS_FIRST>
+__device__ __forceinline__ void or_site_update_hint(const Lattice& L, const Site& c, int parity,
+                                                    const float4* U, float4* G, int i,
+                                                    float omega) {
+  const size_t vh = (size_t)L.vh;
+  const uint64_t pg = l2_policy_evict_last();
+  const HintP Gh{G, pg};
+  Mat3<float> star, gold, gn;
+  if constexpr (LINKS_FIRST)
+    compute_star_12<float, HintP, HintP, NDIR>(L, c, parity, HintP{U, l2_policy_evict_first()},
+                                               Gh, star);
+  else
+    compute_star_12<float, const float4*, HintP, NDIR>(L, c, parity, U, Gh, star);
+  float4* Gp = G + (size_t)parity * 3 * vh;
+  load12_hint(HintP{Gp, pg}, vh, i, gold);
+  or_update_composed(gold, star, omega, gn);
+  store12_hint(Gp, vh, i, gn, pg);
 }
 
 // The FP32 update of site i for two copies of one configuration at once (T = f2):

@@ -28,7 +28,8 @@ struct gfx_ctx {
   int or_block[3];  // OR/SA half-sweep block size, FP32 [0], FP64 [1], double-float [2]
   int or_wide;      // FP32 half-sweep kernel with its full register set (1) or 64 (0)
   int or_pf[3];     // OR half-sweep loads: 0 plain, 1 after an L2 bulk prefetch, 2 plain
-                    // with the odd half-sweep's blocks in reverse order (the default)
+                    // with the odd half-sweep's blocks in reverse order (the default), 3 and
+                    // 4 as 2 with FP32 12-real g as L2 evict_last (4: links evict_first)
   int fuse_check;   // FP32 checks fused into the last odd half-sweep when possible (default 1)
   int odd_checks;   // the FP32-phase checks of a mixed solve may measure the odd sites only
                     // (gfx_or_params.fp32_checks_all_sites = 0); set per gfx_overrelax

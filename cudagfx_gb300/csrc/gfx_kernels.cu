@@ -62,7 +62,10 @@ __global__ void __launch_bounds__(256, WIDE ? 1 : (sizeof(T) == 4 ? 4 : 2)) or_h
   const int i = blk * blockDim.x + threadIdx.x;
   if (i >= L.vh) return;
   const Site c = site_of(L, i, parity);
-  or_site_update<T, NRU, NDIR>(L, c, parity, U, G, i, omega);
+  if constexpr (MODE >= 3 && sizeof(T) == 4 && NRU == 12)
+    or_site_update_hint<NDIR, MODE == 4>(L, c, parity, (const float4*)U, (float4*)G, i, omega);
+  else
+    or_site_update<T, NRU, NDIR>(L, c, parity, U, G, i, omega);
 }
 
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
@@ -76,8 +79,14 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
     if (mode == 1) {
       if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 1, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, 0);
       else or_halfsweep_kernel<float, 12, 3, 1, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, 0);
+    } else if (mode == 3) {
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 3, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+      else or_halfsweep_kernel<float, 12, 3, 3, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+    } else if (mode == 4) {
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 4, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+      else or_halfsweep_kernel<float, 12, 3, 4, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
     } else {
-      const int rev = mode == 2 ? parity : 0;
+      const int rev = mode >= 2 ? parity : 0;
       if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 0, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, rev);
       else or_halfsweep_kernel<float, 12, 3, 0, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, w, rev);
     }
@@ -91,7 +100,7 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
       or_halfsweep_kernel<T, NR, ND, 1><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega, 0);  \
     else                                                                                         \
       or_halfsweep_kernel<T, NR, ND, 0><<<grid, block, 0, s>>>(L, u_, g_, parity, (T)omega,      \
-                                                               mode == 2 ? parity : 0);          \
+                                                               mode >= 2 ? parity : 0);          \
   } while (0)
   if (prec == 2) {  // double-float, 18-real links
     if (ndir == 4) OR_LAUNCH(dfl, 18, 4);
@@ -99,6 +108,17 @@ void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, cons
   } else if (prec == 0 && link_nr == 8) {
     if (ndir == 4) OR_LAUNCH(float, 8, 4);
     else OR_LAUNCH(float, 8, 3);
+  } else if (prec == 0 && mode >= 3) {
+    const float4* u_ = (const float4*)U;
+    float4* g_ = (float4*)G;
+    const float w = (float)omega;
+    if (mode == 3) {
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 3><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+      else or_halfsweep_kernel<float, 12, 3, 3><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+    } else {
+      if (ndir == 4) or_halfsweep_kernel<float, 12, 4, 4><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+      else or_halfsweep_kernel<float, 12, 3, 4><<<grid, block, 0, s>>>(L, u_, g_, parity, w, parity);
+    }
   } else if (prec == 0) {
     if (ndir == 4) OR_LAUNCH(float, 12, 4);
     else OR_LAUNCH(float, 12, 3);

@@ -44,8 +44,8 @@ gfx_status gfx_set_tuning(gfx_ctx* ctx, const gfx_tuning* t) {
   for (int p = 0; p < 2; p++) {
     if (!valid_block(t->block[p]))
       return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: block must be a multiple of 32 in [32, 256]");
-    if (t->staging[p] < 0 || t->staging[p] > 2)
-      return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: staging must be 0, 1 or 2");
+    if (t->staging[p] < 0 || t->staging[p] > 4)
+      return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: staging must be 0 to 4");
   }
   if (t->link_reals64 != 0 && t->link_reals64 != 12 && t->link_reals64 != 18)
     return fail(ctx, GFX_ERR_ARG, "gfx_set_tuning: link_reals64 must be 0, 12 or 18");
@@ -209,7 +209,8 @@ gfx_status gfx_autotune(gfx_ctx* ctx, int gauge, int expected_sweeps, const char
         n = std::min(40, std::max(2, (int)std::ceil(3.0 / std::max(t1, 1e-3))));
       }
       auto sweep = [&]() { enqueue_sweeps(ctx, prec, ndir, 1.7, n); };
-      const int nmodes = 3;
+      // modes 3 and 4 (L2 eviction priorities) exist for the FP32 12-real sweep only
+      const int nmodes = prec == 0 && layouts[li] == 12 ? 5 : 3;
       // FP32 12-real sweeps: both register budgets of the kernel
       const int nwide = prec == 0 && layouts[li] == 12 ? 2 : 1;
       for (int round = 0; round < 2 && s == GFX_OK; round++)

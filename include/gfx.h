@@ -163,8 +163,11 @@ gfx_status gfx_set_block(gfx_ctx *ctx, int block);
  * staging: 0 = plain 128-bit loads; 1 = each block first issues one L2 bulk
  * prefetch (cp.async.bulk.prefetch.L2) per contiguous range it reads; 2 = plain
  * loads, and the odd half-sweep runs its blocks in reverse order, so that it starts
- * on the ranges the even half-sweep touched last (still in L2).  All settings give
- * bit-identical results.
+ * on the ranges the even half-sweep touched last (still in L2); 3 = as 2, with the
+ * FP32 12-real sweep reading and writing g with the L2 eviction priority evict_last;
+ * 4 = as 3, and its links read as evict_first (other sweeps: 3 and 4 act as 2).  A
+ * new context starts with 2, and with 4 for its FP32 sweep when the FP32 g fits in
+ * half the L2 but g and the links together do not fit in it.  All settings give bit-identical results.
  * link_reals64: FP64 link storage, 12 (two rows) or 18 (full).  link_reals32: the
  * FP32 copy the FP32 sweeps read, 12 or 8.  The 8-real form rebuilds rows 1, 2
  * dividing by |U_01|^2 + |U_02|^2; the few links where that is below 1e-2 are read
@@ -193,7 +196,7 @@ gfx_status gfx_get_tuning(const gfx_ctx *ctx, gfx_tuning *out);
  * change of link_reals64 re-packs the FP64 links on the device. */
 gfx_status gfx_set_tuning(gfx_ctx *ctx, const gfx_tuning *t);
 /* Time every candidate setting on this context's lattice and apply the fastest.
- * Candidates: block 64/128/192/256 x staging 0/1/2 for each precision the
+ * Candidates: block 64/128/192/256 x staging 0/1/2 (0-4 for FP32) for each precision the
  * context holds (x both register budgets for FP32), and both link layouts of each
  * precision.  The fields are left as they
  * were: the candidate sweeps run on g and it is restored afterwards.

@@ -1,5 +1,5 @@
 """Launch tuning: every block size, every staging mode (plain loads, L2 bulk prefetch,
-odd half-sweep in reverse block order)
+odd half-sweep in reverse block order, L2 eviction priorities)
 and both FP64 link layouts give bit-identical sweeps; gfx_autotune leaves the fields as it found them, its
 choice reproduces the untuned solve exactly, and its cache file round-trips."""
 import numpy as np
@@ -30,7 +30,7 @@ def test_launch_variants_are_bit_identical(prec):
     for nr in ((12, 18) if prec == 1 else (12,)):
         for wide in ((0, 1) if prec == 0 else (1,)):
             for block in (32, 64, 96, 128, 192, 256):
-                for pf in (0, 1, 2):
+                for pf in (0, 1, 2, 3, 4):
                     c = _ctx()
                     c.set_tuning(block=(block, block), staging=(pf, pf), link_reals64=nr,
                                  wide_regs=wide)
@@ -48,7 +48,7 @@ def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
     ga = a.get_trafo()
     b = _ctx()
     t = b.autotune(expected_sweeps=1000, cache_path=str(tmp_path / "tune.txt"))
-    assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1, 2)
+    assert t["block"][0] in (64, 128, 192, 256) and t["staging"][1] in (0, 1, 2) and t["staging"][0] in range(5)
     assert t["link_reals64"] in (12, 18) and 5 <= t["checkinterval"] <= 100
     assert t["link_reals32"] in (12, 8) and t["wide_regs"] in (0, 1)
     assert t["sweep_ms"][0] > 0 and t["check_ms"][1] > 0
@@ -84,7 +84,7 @@ def test_autotune_cache_hit_applies_stored_settings(tmp_path):
 
 def test_set_tuning_rejects_bad_settings():
     c = _ctx()
-    for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(3, 0)), dict(staging=(0, -1)),
+    for bad in (dict(block=(48, 128)), dict(block=(128, 512)), dict(staging=(5, 0)), dict(staging=(0, -1)),
                 dict(link_reals64=8), dict(link_reals32=18)):
         with pytest.raises(gfx.GfxError):
             c.set_tuning(**bad)
