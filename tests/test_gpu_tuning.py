@@ -147,3 +147,14 @@ def test_fp32_link8_solve_reaches_the_same_copy():
         res.append(r.final_values.F)
         c.close()
     assert abs(res[0] - res[1]) < 1e-11
+
+
+@pytest.mark.parametrize("dims,want", [((32, 32, 32, 32), 4), ((24, 24, 24, 24), 2),
+                                       ((32, 32, 32, 48), 2)])
+def test_default_staging_keeps_g_in_l2_where_it_fits(dims, want):
+    # the FP32 sweep starts with g kept in L2 (staging 4) when its 48 B per site fit in
+    # half of the L2 but links and g (240 B per site) do not: on GB300's 126 MB L2 that
+    # is 32^4, not 24^4 (all of it fits) nor 32^3 x 48 (g is 75 MB)
+    c = gfx.Context(dims, precision=gfx.PREC_MIXED)
+    assert c.tuning()["staging"] == [want, 2]
+    c.close()
