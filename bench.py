@@ -82,6 +82,9 @@ def parse():
                     help="copies of the 16^4 (beta 6.0) and 24^4 (beta 6.2) configurations")
     ap.add_argument("--gribov-paired", action="store_true",
                     help="batched FP32 sweeps with two copies per thread (packed FP32)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="Gribov copies: one warm-up and one timed batched solve, without the "
+                         "other sweep kernel and the sequential arms (for profiler captures)")
     ap.add_argument("--config", choices=["c1", "c2", "c3", "c4", "c5"], default=None,
                     help="instead of the bench: one full workload, mixed against all-FP64 "
                          "(--no-fp64 skips that solve): c1 8^4 (also on the CPU oracle), c2 "
@@ -166,11 +169,13 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
         b.set_links(bi, links[k])
     # the other FP32 sweep kernel first, for comparison: two copies per thread (packed
     # FP32) unless --gribov-paired makes that the measured one
-    b.set_paired(0 if args.gribov_paired else 1)
-    starts()
-    b.overrelax(**kw)  # warm-up (graph instantiation)
-    starts()
-    _, ms_b1 = b.overrelax(**kw)
+    ms_b1 = None
+    if not args.batch_only:
+        b.set_paired(0 if args.gribov_paired else 1)
+        starts()
+        b.overrelax(**kw)  # warm-up (graph instantiation)
+        starts()
+        _, ms_b1 = b.overrelax(**kw)
     b.set_paired(1 if args.gribov_paired else 0)
     starts()
     b.overrelax(**kw)
@@ -183,6 +188,12 @@ def gribov_batch(args, gfx, mt_source, rank=0, ws=1, dist=None):
             local_best[k] = (f, mine[k][j])
     upd = sum(r["sweeps"] * int(np.prod(confs[held[r["conf"]]][0])) for r in res)
     b.close()
+    if args.batch_only:
+        ms_b, upd = max_over_ranks(dist, ms_b), sum_over_ranks(dist, upd)
+        return {"workload": "%d x 16^4 (beta 6.0) + %d x 24^4 (beta 6.2) Gribov copies, Haar "
+                            "starts, theta<%g, batched solve only" % (ncopies[0], ncopies[1], args.eps),
+                "batched_s": ms_b / 1000.0, "batched_site_updates_per_s": upd / (ms_b / 1000.0),
+                "converged": int(sum_over_ranks(dist, sum(r["converged"] for r in res)))}
     # sequential arms: the single-lattice solver per copy, (a) its device loop captured
     # in a CUDA graph (the strict comparison), (b) launched kernel by kernel with a host
     # check every checkinterval sweeps, the structure of the reference's overrelax_gauge
