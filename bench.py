@@ -237,9 +237,9 @@ def run_kernels(args, dims):
     """A short fixed workload for profiler captures: 3 FP32 OR sweeps, an FP32 and an
     FP64 functional, 31 sweeps of the FP32 convergence loop with a check every 10 (the
     fused check), 1 FP64 OR sweep, 3 rebased FP32 sweeps and their functional, one
-    SA step with one microcanonical step, and one link-heatbath sweep in FP64 and one in
-    FP32 arithmetic.  The OR sweeps use --staging (2, the tuner's
-    choice on 32^4: the odd half-sweep in reverse block order)."""
+    SA step with one microcanonical step, one link-heatbath sweep in FP64 and one in
+    FP32 arithmetic, the plaquette and the Polyakov loop.  The OR sweeps use --staging
+    (2, the odd half-sweep in reverse block order, unless given)."""
     import cudagfx_gb300 as gfx
     V = int(np.prod(dims))
     ctx = gfx.Context(dims, precision=gfx.PREC_MIXED)
@@ -267,6 +267,8 @@ def run_kernels(args, dims):
     ctx.simanneal(0.5, 0.5, 1, nmicro=1)
     ctx.thermalize(args.beta, 1, variant=gfx.HB_KENNEDY_PENDLETON)
     ctx.thermalize(args.beta, 1, variant=gfx.HB_KENNEDY_PENDLETON, precision=1)
+    ctx.plaquette()
+    ctx.polyakov()
     ctx.close()
     print("kernels ok")
 
