@@ -417,11 +417,13 @@ gfx_status gfx_create(gfx_ctx** out, int lx, int ly, int lz, int lt, int precisi
     // in half of it, g is kept there (evict_last) while the links pass as evict_first:
     // 4% faster FP32 sweeps on 32^4 (48 MB of g, 126 MB of L2)
     int dev = 0, l2 = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess &&
-        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) == cudaSuccess &&
-        (double)vol * 48.0 <= 0.5 * (double)l2 && (double)vol * 240.0 > (double)l2)
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess) {
+      cudaGetLastError();  // this query's own failure; the default stays 2
+      l2 = 0;
+    }
+    if (l2 > 0 && (double)vol * 48.0 <= 0.5 * (double)l2 && (double)vol * 240.0 > (double)l2)
       ctx->or_pf[0] = 4;
-    cudaGetLastError();
   }
   ctx->or_wide = 1;
   ctx->fuse_check = 1;
