@@ -122,9 +122,10 @@ typedef struct {
   double beta;
   int variant; /* GFX_HB_REFERENCE or GFX_HB_KENNEDY_PENDLETON */
   int precision; /* 0: FP64 arithmetic (the reference's); 1: FP32 staples and SU(2)
-                    steps from the FP32 link copy, FP64 reunitarization of each new
-                    link (SINGLE or MIXED contexts; the same distribution, on the
-                    FP32 units) */
+                    steps from the FP32 link copy, each new link reunitarized in
+                    double-float (unitary to ~1e-14) and stored in FP64 and FP32
+                    (SINGLE or MIXED contexts; the same distribution, on the FP32
+                    units) */
 } gfx_therm_params;
 
 /* Link-heatbath variants.  REFERENCE reproduces the reference's update
