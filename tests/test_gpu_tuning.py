@@ -39,6 +39,21 @@ def test_launch_variants_are_bit_identical(prec):
                     c.close()
 
 
+def test_fp32_staging_modes_bit_identical_in_coulomb_gauge():
+    # the three-direction FP32 kernels of every staging mode, both register budgets
+    ref = _ctx()
+    ref.or_sweeps(3, omega=1.7, gauge=gfx.COULOMB, precision=0)
+    want = ref.get_trafo()
+    ref.close()
+    for wide in (0, 1):
+        for pf in (0, 1, 2, 3, 4):
+            c = _ctx()
+            c.set_tuning(block=(64, 64), staging=(pf, pf), wide_regs=wide)
+            c.or_sweeps(3, omega=1.7, gauge=gfx.COULOMB, precision=0)
+            assert np.array_equal(c.get_trafo(), want), (wide, pf)
+            c.close()
+
+
 def test_autotune_keeps_fields_and_reproduces_solve(tmp_path):
     kw = dict(maxit=3000, eps=1e-12, checkinterval=20, omega=1.7, criterion=gfx.CRIT_THETA)
     a = _ctx()
