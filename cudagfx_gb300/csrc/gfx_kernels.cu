@@ -39,8 +39,10 @@ Lattice make_lattice(int lx, int ly, int lz, int lt) {
 // ---------------------------------------------------------------------------
 // overrelaxation half-sweep (overrelax.cu:335-446), in place on parity `parity`
 // ---------------------------------------------------------------------------
-// MODE (launch_or_halfsweep's mode 0/1): 0 plain loads; 1 each block first issues one
-// L2 bulk prefetch per contiguous range it reads.  rev != 0 runs the blocks in reverse
+// MODE (launch_or_halfsweep's mode): 0 plain loads (modes 0 and 2); 1 each block first
+// issues one L2 bulk prefetch per contiguous range it reads; 3 and 4 (FP32 12-real
+// only) read and write g with the L2 eviction priority evict_last, 4 also reads the
+// links as evict_first (or_site_update_hint).  rev != 0 runs the blocks in reverse
 // index order: after a half-sweep in forward order, the next one then starts on the
 // ranges the previous one touched last, which L2 may still hold.  The sites of one
 // parity are independent, so the order does not change the result.
