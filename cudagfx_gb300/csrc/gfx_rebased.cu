@@ -4,6 +4,7 @@
 #include <algorithm>
 
 #include "gfx_internal.h"
+#include "gfx_narrow.h"
 #include "gfx_rebased.cuh"
 
 namespace gfx {
@@ -11,8 +12,30 @@ namespace gfx {
 constexpr int kRebasedBlock = 128;
 
 // ---------------------------------------------------------------------------
-// base construction (FP64)
+// base construction, in double-float on the FP32 units
 // ---------------------------------------------------------------------------
+// GB300 runs FP64 at 1/64 of its FP32 rate: the base built in FP64 took the FP64 pipe
+// to 87-95% (3.1 ms on 32^4, 8% of a batched Gribov solve with a base per copy).  The
+// FP64 links and g are split into double-float pairs on the integer units
+// (gfx_narrow.h, bit for bit hi = (float)d, lo = (float)(d - hi)) and the products and
+// sums run in double-float (~2^-46; the stored pairs hold ~2^-48).
+
+// an FP64 matrix of NC double2 planes (6: rows 0,1, row 2 rebuilt; 9: all rows) as
+// double-float pairs
+template <int NC>
+__device__ __forceinline__ void load_narrow(const double2* __restrict__ base, size_t stride,
+                                            int i, Mat3<dfl>& m) {
+#pragma unroll
+  for (int k = 0; k < NC; k++) {
+    const double2 v = __ldg(base + k * stride + i);
+    float rh, rl, ih, il;
+    narrow_df(v.x, rh, rl);
+    narrow_df(v.y, ih, il);
+    m.e[k / 3][k % 3] = cmk<dfl>(dfl(rh, rl), dfl(ih, il));
+  }
+  if (NC == 6) row2_from_01(m);
+}
+
 // U'_mu(x) = g(x) U_mu(x) g(x+mu)^+ for mu = blockIdx.z: rows 0,1 as an FP32 value (Ur,
 // the 12-real FP32 link layout) and the FP32 remainder (Ulo, the same layout)
 template <int NR>
@@ -26,26 +49,26 @@ __global__ void __launch_bounds__(128) rebase_links_kernel(Lattice L, const doub
   constexpr int NC = Field<double, NR>::NCHUNK;
   const size_t vh = (size_t)L.vh;
   const Site c = site_of(L, i, parity);
-  Mat3<double> g, gn, u;
-  Field<double, 12>::load(G + (size_t)parity * 6 * vh, vh, i, g);
-  Field<double, NR>::load(U + (size_t)(parity * 4 + mu) * NC * vh, vh, i, u);
-  Field<double, 12>::load(G + (size_t)(1 - parity) * 6 * vh, vh, nb_fwd(L, c, mu), gn);
+  Mat3<dfl> g, gn, u;
+  load_narrow<6>(G + (size_t)parity * 6 * vh, vh, i, g);
+  load_narrow<NC>(U + (size_t)(parity * 4 + mu) * NC * vh, vh, i, u);
+  load_narrow<6>(G + (size_t)(1 - parity) * 6 * vh, vh, nb_fwd(L, c, mu), gn);
   float hi[12], lo[12];
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    cplx<double> h[3];
+    cplx<dfl> h[3];
 #pragma unroll
     for (int k = 0; k < 3; k++) h[k] = mul_entry(g, u, a, k);
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-      cplx<double> x = cmulc(h[0], gn.e[j][0]);
+      cplx<dfl> x = cmulc(h[0], gn.e[j][0]);
       cmacc(x, h[1], gn.e[j][1]);
       cmacc(x, h[2], gn.e[j][2]);
       const int k = 2 * (3 * a + j);
-      hi[k] = (float)x.re;
-      hi[k + 1] = (float)x.im;
-      lo[k] = (float)(x.re - (double)hi[k]);
-      lo[k + 1] = (float)(x.im - (double)hi[k + 1]);
+      hi[k] = x.re.hi;
+      hi[k + 1] = x.im.hi;
+      lo[k] = x.re.lo;
+      lo[k + 1] = x.im.lo;
     }
   }
   const size_t off = (size_t)(parity * 4 + mu) * 3 * vh + i;
@@ -56,10 +79,10 @@ __global__ void __launch_bounds__(128) rebase_links_kernel(Lattice L, const doub
   }
 }
 
-// rows 0,1 of a rebased link as hi + lo in FP64, row 2 = conj(row0 x row1)
-__device__ __forceinline__ void load_rebased64(const float4* __restrict__ hi,
-                                               const float4* __restrict__ lo, size_t vh, int i,
-                                               Mat3<double>& m) {
+// rows 0,1 of a rebased link as double-float pairs hi + lo, row 2 = conj(row0 x row1)
+__device__ __forceinline__ void load_rebased_df(const float4* __restrict__ hi,
+                                                const float4* __restrict__ lo, size_t vh, int i,
+                                                Mat3<dfl>& m) {
   float h[12], l[12];
 #pragma unroll
   for (int p = 0; p < 3; p++) {
@@ -72,12 +95,12 @@ __device__ __forceinline__ void load_rebased64(const float4* __restrict__ hi,
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       const int k = 2 * (3 * r + c);
-      m.e[r][c] = cmk<double>((double)h[k] + (double)l[k], (double)h[k + 1] + (double)l[k + 1]);
+      m.e[r][c] = cmk<dfl>(dfl(h[k], l[k]), dfl(h[k + 1], l[k + 1]));
     }
   row2_from_01(m);
 }
 
-// w0(x) = sum_mu U'_mu(x) + U'_mu(x-mu)^+ in FP64, stored split (see kW0Planes)
+// w0(x) = sum_mu U'_mu(x) + U'_mu(x-mu)^+ in double-float, stored split (see kW0Planes)
 template <int NDIR>
 __global__ void __launch_bounds__(128) rebase_star_kernel(Lattice L, const float4* __restrict__ Ur,
                                                           const float4* __restrict__ Ulo,
@@ -88,44 +111,46 @@ __global__ void __launch_bounds__(128) rebase_star_kernel(Lattice L, const float
   const size_t vh = (size_t)L.vh;
   const Site c = site_of(L, i, parity);
   const int q = 1 - parity;
-  Mat3<double> w;
+  Mat3<dfl> w;
   mzero(w);
 #pragma unroll
   for (int mu = 0; mu < NDIR; mu++) {
-    Mat3<double> u;
+    Mat3<dfl> u;
     const size_t fo = (size_t)(parity * 4 + mu) * 3 * vh, bo = (size_t)(q * 4 + mu) * 3 * vh;
-    load_rebased64(Ur + fo, Ulo + fo, vh, i, u);
+    load_rebased_df(Ur + fo, Ulo + fo, vh, i, u);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
       for (int k = 0; k < 3; k++) w.e[r][k] = cadd(w.e[r][k], u.e[r][k]);
-    load_rebased64(Ur + bo, Ulo + bo, vh, nb_bwd(L, c, mu), u);
+    load_rebased_df(Ur + bo, Ulo + bo, vh, nb_bwd(L, c, mu), u);
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
       for (int k = 0; k < 3; k++) w.e[r][k] = cadd(w.e[r][k], cconj(u.e[k][r]));
   }
+  // hi: the FP32 star; the remainders (|lo| <= ulp(hi)/2) enter only through their
+  // anti-hermitian part and trace
   float f[28];
-  Mat3<double> lo;
+  Mat3<float> lo;
 #pragma unroll
   for (int r = 0; r < 3; r++)
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       const int j = 2 * (3 * r + k);
-      f[j] = (float)w.e[r][k].re;
-      f[j + 1] = (float)w.e[r][k].im;
-      lo.e[r][k] = cmk<double>(w.e[r][k].re - (double)f[j], w.e[r][k].im - (double)f[j + 1]);
+      f[j] = w.e[r][k].re.hi;
+      f[j + 1] = w.e[r][k].im.hi;
+      lo.e[r][k] = cmk<float>(w.e[r][k].re.lo, w.e[r][k].im.lo);
     }
-  f[18] = (float)lo.e[0][0].im;
-  f[19] = (float)lo.e[1][1].im;
-  f[20] = (float)lo.e[2][2].im;
-  f[21] = (float)(0.5 * (lo.e[0][1].re - lo.e[1][0].re));
-  f[22] = (float)(0.5 * (lo.e[0][1].im + lo.e[1][0].im));
-  f[23] = (float)(0.5 * (lo.e[0][2].re - lo.e[2][0].re));
-  f[24] = (float)(0.5 * (lo.e[0][2].im + lo.e[2][0].im));
-  f[25] = (float)(0.5 * (lo.e[1][2].re - lo.e[2][1].re));
-  f[26] = (float)(0.5 * (lo.e[1][2].im + lo.e[2][1].im));
-  f[27] = (float)(lo.e[0][0].re + lo.e[1][1].re + lo.e[2][2].re);
+  f[18] = lo.e[0][0].im;
+  f[19] = lo.e[1][1].im;
+  f[20] = lo.e[2][2].im;
+  f[21] = 0.5f * (lo.e[0][1].re - lo.e[1][0].re);
+  f[22] = 0.5f * (lo.e[0][1].im + lo.e[1][0].im);
+  f[23] = 0.5f * (lo.e[0][2].re - lo.e[2][0].re);
+  f[24] = 0.5f * (lo.e[0][2].im + lo.e[2][0].im);
+  f[25] = 0.5f * (lo.e[1][2].re - lo.e[2][1].re);
+  f[26] = 0.5f * (lo.e[1][2].im + lo.e[2][1].im);
+  f[27] = lo.e[0][0].re + lo.e[1][1].re + lo.e[2][2].re;
   float4* out = W0 + (size_t)parity * kW0Planes * vh + i;
 #pragma unroll
   for (int p = 0; p < kW0Planes; p++)
