@@ -7,6 +7,7 @@
 
 #include "gfx_device.cuh"
 #include "gfx_internal.h"
+#include "gfx_narrow.h"
 #include "gfx_pair.cuh"
 
 namespace gfx {
@@ -35,6 +36,22 @@ struct Load<double, float, 12> {
     normalize<double, true>(m);
   }
 };
+
+// an FP64 matrix of NC double2 planes (6: rows 0,1, row 2 rebuilt; 9: all rows) as
+// double-float pairs, split on the integer units (gfx_narrow.h)
+template <int NC>
+__device__ __forceinline__ void load_narrow(const double2* __restrict__ base, size_t stride,
+                                            int i, Mat3<dfl>& m) {
+#pragma unroll
+  for (int k = 0; k < NC; k++) {
+    const double2 v = __ldg(base + k * stride + i);
+    float rh, rl, ih, il;
+    narrow_df(v.x, rh, rl);
+    narrow_df(v.y, ih, il);
+    m.e[k / 3][k % 3] = cmk<dfl>(dfl(rh, rl), dfl(ih, il));
+  }
+  if (NC == 6) row2_from_01(m);
+}
 
 // ---------------------------------------------------------------------------
 // L2 warm-up for one block of checkerboard sites [i0, i0 + n) of one parity.

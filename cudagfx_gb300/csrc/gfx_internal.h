@@ -71,7 +71,8 @@ struct Reduced {
 void launch_or_halfsweep(int prec, int link_nr, int ndir, const Lattice& L, const void* U, void* G,
                          int parity, double omega, int block, int mode, cudaStream_t s,
                          int wide = 0);
-// measure: compute precision (0 float, 1 double), g storage (0 float, 1 double)
+// measure: compute precision (0 float, 1 double, 2 double-float fields), g storage (0
+// float, 1 double, 2 double-float)
 void launch_measure(int cprec, int link_nr, int gprec, int ndir, const Lattice& L, const void* U,
                     const void* G, double* partials, int block, cudaStream_t s);
 int measure_blocks_x(const Lattice& L, int block);

@@ -4,7 +4,6 @@
 #include <algorithm>
 
 #include "gfx_internal.h"
-#include "gfx_narrow.h"
 #include "gfx_rebased.cuh"
 
 namespace gfx {
@@ -19,22 +18,6 @@ constexpr int kRebasedBlock = 128;
 // FP64 links and g are split into double-float pairs on the integer units
 // (gfx_narrow.h, bit for bit hi = (float)d, lo = (float)(d - hi)) and the products and
 // sums run in double-float (~2^-46; the stored pairs hold ~2^-48).
-
-// an FP64 matrix of NC double2 planes (6: rows 0,1, row 2 rebuilt; 9: all rows) as
-// double-float pairs
-template <int NC>
-__device__ __forceinline__ void load_narrow(const double2* __restrict__ base, size_t stride,
-                                            int i, Mat3<dfl>& m) {
-#pragma unroll
-  for (int k = 0; k < NC; k++) {
-    const double2 v = __ldg(base + k * stride + i);
-    float rh, rl, ih, il;
-    narrow_df(v.x, rh, rl);
-    narrow_df(v.y, ih, il);
-    m.e[k / 3][k % 3] = cmk<dfl>(dfl(rh, rl), dfl(ih, il));
-  }
-  if (NC == 6) row2_from_01(m);
-}
 
 // U'_mu(x) = g(x) U_mu(x) g(x+mu)^+ for mu = blockIdx.z: rows 0,1 as an FP32 value (Ur,
 // the 12-real FP32 link layout) and the FP32 remainder (Ulo, the same layout)
