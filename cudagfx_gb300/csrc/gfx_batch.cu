@@ -98,6 +98,47 @@ __global__ void __launch_bounds__(kBatchBlock, sizeof(T) == 4 ? 8 : 4) or_batch_
   or_site_update<T, 12, NDIR>(C.L, s, parity, U, G, i, omega);
 }
 
+// The last odd half-sweep before an FP32 check (or_batch_kernel<float> with parity 1),
+// writing the check's partials of the configurations whose FP32-phase checks read the
+// odd sites only (BConf::odd_only), as or_halfsweep_measure_kernel does for one
+// lattice: the odd sites' star depends on the even sites only, so the partials are
+// those measure_batch_kernel would form after the sweep, bit for bit.  With odd_only
+// the slice holds whole 128-site blocks, so every block is full and lies in one slice.
+template <int NDIR>
+__global__ void __launch_bounds__(kBatchBlock, 6) or_batch_measure_kernel(BDesc d, float omega) {
+  const int parity = 1;
+  const int item = (int)gridDim.x - 1 - (int)blockIdx.x;  // parity 1's order
+  const int ci = conf_of(d, item, &BConf::item_base);
+  const BConf& C = d.c[ci];
+  const int local = item - C.item_base;
+  const int blk = local / C.ncopies, copy = local - blk * C.ncopies;
+  if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
+  const int i = blk * kBatchBlock + threadIdx.x;
+  const float4* U = (const float4*)C.U32;
+  float4* G = (float4*)C.G32 + (size_t)copy * C.gstride32;
+  if (!C.odd_only) {  // uniform over the block: the sweep alone
+    if (i >= C.L.vh) return;
+    or_site_update<float, 12, NDIR>(C.L, site_of(C.L, i, parity), parity, U, G, i, omega);
+    return;
+  }
+  const size_t vh = (size_t)C.L.vh;
+  const Site s = site_of(C.L, i, parity);
+  float4* Gp = G + (size_t)parity * 3 * vh;
+  Mat3<float> star, gold, gn;
+  compute_star_f32<NDIR>(C.L, s, parity, U, G, star);
+  Field<float, 12>::load(Gp, vh, i, gold);
+  or_update_composed(gold, star, omega, gn);
+  Field<float, 12>::store(Gp, vh, i, gn);
+  row2_from_01(gn);  // as the measurement's load of the stored rows
+  float f, dd;
+  site_functional_f32(gn, star, f, dd);
+  const int t = blk / C.nbx, bx = blk - t * C.nbx;
+  const int per_copy = 2 * C.L.lt * C.nbx;
+  block_reduce3_f32(f, dd,
+                    d.partials + 3 * (C.part_base + (size_t)copy * per_copy +
+                                      (size_t)(parity * C.L.lt + t) * C.nbx + bx));
+}
+
 // The FP32 half-sweep with two copies per thread (or_site_update_pair: packed FP32
 // arithmetic, lane for lane the operations of or_batch_kernel<float>).  Work items are
 // (configuration, site block, copy pair), pair-minor, so the pairs of a site block run
@@ -162,8 +203,9 @@ __global__ void __launch_bounds__(kBatchBlock, 4) or_batch_rebased_kernel(BDesc 
 }
 
 // Per-copy functional partials (measure_kernel per copy, same block grouping)
+// fused: the FP32 partials of odd_only configurations came from or_batch_measure_kernel
 template <typename TC, typename TSG, int NDIR>
-__global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
+__global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d, int fused) {
   const int ci = conf_of(d, blockIdx.x, &BConf::mitem_base);
   const BConf& C = d.c[ci];
   int local = blockIdx.x - C.mitem_base;
@@ -175,7 +217,8 @@ __global__ void __launch_bounds__(kBatchBlock) measure_batch_kernel(BDesc d) {
   const int t = local / C.nbx, bx = local - t * C.nbx;
   if (d.states[C.copy_base + copy].done != 0) return;  // uniform over the block
   constexpr bool F32 = sizeof(TC) == 4 && sizeof(TSG) == 4;
-  if (F32 && C.odd_only && parity == 0) return;  // the FP32-phase checks: odd sites only
+  // the FP32-phase checks: odd sites only, and those already written by a fused sweep
+  if (F32 && C.odd_only && (parity == 0 || fused)) return;
   typedef typename VecOf<TC>::type VU;
   typedef typename VecOf<TSG>::type VG;
   const VU* U = (const VU*)(sizeof(TC) == 4 ? C.U32 : C.U64);
@@ -417,10 +460,17 @@ gfx_status balloc(gfx_batch* b, void** p, size_t bytes) {
   return GFX_OK;
 }
 
-void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega) {
+// last: the sweep before a check; FP32 one copy per thread then writes the check's odd
+// partials in its odd half-sweep (or_batch_measure_kernel)
+void enqueue_sweep(gfx_batch* b, int prec, int ndir, double omega, bool last = false) {
   const size_t sm = 0;
   for (int p = 0; p < 2; p++) {
-    if (prec == 3) {  // rebased FP32
+    if (prec == 0 && !b->paired && last && p == 1) {
+      if (ndir == 4)
+        or_batch_measure_kernel<4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, (float)omega);
+      else
+        or_batch_measure_kernel<3><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, (float)omega);
+    } else if (prec == 3) {  // rebased FP32
       if (ndir == 4)
         or_batch_rebased_kernel<4><<<b->nitems, kBatchBlock, sm, b->stream>>>(b->desc, p, (float)omega);
       else
@@ -450,14 +500,21 @@ void enqueue_check(gfx_batch* b, int cprec, int gprec, int ndir, int advance,
     if (ndir == 4) measure_batch_rebased_kernel<4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
     else measure_batch_rebased_kernel<3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
   } else if (cprec == 0) {
-    if (ndir == 4) measure_batch_kernel<float, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
-    else measure_batch_kernel<float, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    const int fused = b->paired ? 0 : 1;
+    bool all_fused = fused != 0;
+    for (int c = 0; c < b->nconf; c++) all_fused &= b->desc.c[c].odd_only != 0;
+    if (!all_fused) {
+      if (ndir == 4)
+        measure_batch_kernel<float, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, fused);
+      else
+        measure_batch_kernel<float, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, fused);
+    }
   } else if (gprec == 0) {
-    if (ndir == 4) measure_batch_kernel<double, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
-    else measure_batch_kernel<double, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    if (ndir == 4) measure_batch_kernel<double, float, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, 0);
+    else measure_batch_kernel<double, float, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, 0);
   } else {
-    if (ndir == 4) measure_batch_kernel<double, double, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
-    else measure_batch_kernel<double, double, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc);
+    if (ndir == 4) measure_batch_kernel<double, double, 4><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, 0);
+    else measure_batch_kernel<double, double, 3><<<b->nmitems, kBatchBlock, 0, b->stream>>>(b->desc, 0);
   }
   slice_batch_kernel<<<b->nsitems, 256, 0, b->stream>>>(b->desc, cprec == 0 && gprec == 0);
   check_batch_kernel<<<b->ncopies, 256, 0, b->stream>>>(b->desc, ndir, advance);
@@ -497,7 +554,7 @@ gfx_status get_graph(gfx_batch* b, int prec, int ndir, int ck, double omega,
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   BCK(cudaStreamBeginCaptureToGraph(b->stream, body, nullptr, nullptr, 0,
                                     cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega);
+  for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega, k == ck - 1);
   enqueue_check(b, prec, prec, ndir, ck, (unsigned long long)handle, 1);
   cudaGraph_t cap;
   cudaError_t e = cudaStreamEndCapture(b->stream, &cap);
@@ -523,7 +580,7 @@ gfx_status run_phase(gfx_batch* b, int prec, int ndir, int ck, double omega, int
   }
   int running = 1;
   while (running > 0) {
-    for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega);
+    for (int k = 0; k < ck; k++) enqueue_sweep(b, prec, ndir, omega, k == ck - 1);
     enqueue_check(b, prec, prec, ndir, ck, 0, 0);
     BCK(cudaGetLastError());
     BCK(cudaMemcpyAsync(&running, b->running, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
@@ -859,7 +916,7 @@ gfx_status gfx_batch_overrelax(gfx_batch* b, const gfx_or_params* pin, gfx_copy_
   // FP32 sweeps start from the FP32 copy of g (g_64_to_32 per copy)
   if (prec0 == 0) convert_batch_kernel<<<cgrid, 128, 0, b->stream>>>(b->desc, 0, -1);
   // iteration 0: sweep, then the first check (advance 0), as overrelax_gauge
-  enqueue_sweep(b, prec0, ndir, p.omega);
+  enqueue_sweep(b, prec0, ndir, p.omega, true);
   enqueue_check(b, prec0, prec0, ndir, 0, 0, 0);
   BCK(cudaGetLastError());
   if ((s = read_states(b))) return s;

@@ -19,8 +19,9 @@ def _free_port():
 
 def _rank_main(rank, ws, port, out):
     sys.path.insert(0, ROOT)
+    # the ranks run on the CPU (gloo), also on a machine with fewer GPUs than ranks
     os.environ.update(RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE=str(ws),
-                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), CUDA_VISIBLE_DEVICES="")
     import bench
     r, w, local, dist = bench.dist_init(None)
     assert (r, w, local) == (rank, ws, rank)
